@@ -1,0 +1,365 @@
+"""FLIP step throughput on one GB300 (replicas on N GPUs).
+
+Workload (default): the 256^3 dam break -- block x<0.4, y<0.6, all z, walls
+on all faces, 8 particles per fluid cell from seed 0, gravity -9.8 with
+dx=1/256 (9.8*256 cells/s^2 in index space), flip 0.95, CFL 1, 30 frames/s,
+fp32 Jacobi PCG to relative residual 1e-5 (max 1500 iterations).  A step is
+one FlipDriver::RunOneStep with dt from the CFL rule.
+
+value: steps/s with the particle state resident in HBM, CUDA events on the
+library's stream around exactly K steps (after W warm-up steps), max over
+ranks.  The particle state (32.2M particles, 1.16 GB) is larger than L2.
+e2e:   the same steps through the public C ABI from pinned host buffers:
+upload particles (H2D), step, download particles (D2H) every step.
+roofline: the dominant kernel's algorithmic bytes / its event-timed time.
+cpu_baseline: the oracle (a restatement of the reference CPU path, single
+thread, as the reference runs one partition with TBB at 1 thread) timed on
+the host for a bounded sample of the same workload.
+
+--impl reference times that CPU path alone (the reference itself cannot be
+built here) and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "fluid-sim-lb_gb300"))
+sys.path.insert(0, str(ROOT))
+
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+FRAME_STEP = float(np.float32(1.0) / np.float32(30.0))
+
+WORKLOADS = {
+    "dam_break_256": dict(n=256, scene="dam_break"),
+    "sphere_drop_64": dict(n=64, scene="sphere_drop"),
+    "sphere_drop_128": dict(n=128, scene="sphere_drop"),
+    "multidam_512": dict(n=512, scene="multidam"),
+    "sphere_pool_1024": dict(n=1024, scene="sphere_pool"),
+}
+
+# Algorithmic HBM bytes per fluid cell (DOF) per launch of each PCG kernel:
+#   pcg_spmv:   read r, p_old (8) + flags (1); write p, Ap (8)        = 17 B
+#   pcg_update: read x, p, r, Ap (16) + flags (1); write x, r (8)     = 25 B
+ALG_BYTES = {"pcg_spmv": 17, "pcg_update": 25, "pcg_spmv_mixed": 17, "pcg_update_mixed": 25}
+
+
+def peaks():
+    try:
+        d = json.loads(PEAKS.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, dev: int):
+        self.dev = dev
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def pcg_cfg(args):
+    import fsim
+
+    prec = {"fp32": fsim.PREC_FP32, "mixed": fsim.PREC_MIXED, "fp64": fsim.PREC_FP64}[args.precision]
+    return fsim.pcg_params(fsim.PCG_RELATIVE, prec, args.max_iterations, tolerance=args.tol,
+                           inner_tolerance=1e-3)
+
+
+def make_sim(wl, args, device):
+    import fsim
+
+    n = wl["n"]
+    g, f = fsim.physical_gravity(n)
+    sim = fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8, device=device)
+    sim.seed(fsim.scene_passes(wl["scene"], n), seed=0)
+    return sim
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    import fsim
+
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(device)
+    wl = WORKLOADS[args.workload]
+    sim = make_sim(wl, args, device)
+    n_particles = sim.particle_count()
+    prm = pcg_cfg(args)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=device)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up steps (untimed)
+    t_in_frame = 0.0
+    inv = sim.cfl()
+
+    def next_dt():
+        nonlocal t_in_frame, inv
+        dt, t_in_frame = fsim.compute_dt(inv, 1, FRAME_STEP, t_in_frame)
+        if t_in_frame + 1e-5 >= FRAME_STEP:
+            t_in_frame = 0.0
+        return dt
+
+    for _ in range(args.warmup):
+        st = sim.step(next_dt(), prm)
+        inv = st.next_inv_speed
+    sim.set_profiling(True)
+    sim.reset_kernel_times()
+    launches0 = sim.launch_count()
+    iters, rows = [], []
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(device) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            st = sim.step(next_dt(), prm)
+            inv = st.next_inv_speed
+            iters.append(st.pcg.iterations)
+            rows.append(st.pcg.n_rows)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    kt = sim.kernel_times()
+    launches = sim.launch_count() - launches0
+    sim.set_profiling(False)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    n_fluid = float(np.mean(rows)) if rows else None
+
+    # e2e: public API with host buffers (pinned), H2D + step + D2H per step
+    pos, vel, gvel = sim.download_particles()
+    hp = torch.from_numpy(pos).pin_memory()
+    hv = torch.from_numpy(vel).pin_memory()
+    hg = torch.from_numpy(gvel).pin_memory()
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        sim.lib.fsim_upload_particles(sim.h, hp.data_ptr(), hv.data_ptr(), hg.data_ptr(),
+                                      hp.shape[0])
+        st = sim.step(next_dt(), prm)
+        inv = st.next_inv_speed
+        cnt = sim.particle_count()
+        import ctypes as C
+
+        got = C.c_int64()
+        rc = sim.lib.fsim_download_particles(sim.h, hp.data_ptr(), hv.data_ptr(), hg.data_ptr(),
+                                             hp.shape[0], C.byref(got))
+        if rc:
+            raise RuntimeError(sim.lib.fsim_last_error(sim.h).decode())
+        if cnt < hp.shape[0]:  # particles deleted at walls: shrink the state
+            hp, hv, hg = hp[:cnt], hv[:cnt], hg[:cnt]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    barrier()
+    sim.close()
+    return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, clocks=clk.summary(),
+                n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms,
+                e2e_bytes=36 * n_particles)
+
+
+def roofline(res):
+    peak, src = peaks()
+    kt = res["kt"]
+    if not kt:
+        return None
+    top = max(kt.items(), key=lambda kv: kv[1][0])
+    name, (tot_ms, nl) = top
+    total_iters = sum(res["iters"])
+    # bytes of each working launch = per-DOF bytes x that step's unknowns
+    out = {"bound": "hbm", "kernel": name, "peak": peak, "peak_source": src, "unit": "GB/s",
+           "share_of_step": tot_ms / res["ms"] if res["ms"] > 0 else None, "traffic": None}
+    if name in ALG_BYTES and res["n_fluid"]:
+        alg = ALG_BYTES[name] * res["n_fluid"]  # per working launch (mean unknowns)
+        tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["rows"], res["iters"]))
+        achieved = tot_bytes / (tot_ms * 1e-3) / 1e9
+        out.update(achieved=achieved, frac=achieved / peak,
+                   alg_bytes_per_launch=alg, working_launches=total_iters, launches=nl)
+    else:
+        out.update(achieved=None, frac=None, launches=nl)
+    return out
+
+
+def cpu_sample(args):
+    """The oracle on a bounded sample of the same workload (single thread)."""
+    import fsim
+    from oracle.oracle import OracleSim
+
+    wl = WORKLOADS[args.workload]
+    n = wl["n"]
+    g, f = fsim.physical_gravity(n)
+    orc = OracleSim((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8)
+    orc.seed(fsim.scene_passes(wl["scene"], n), seed=0)
+    t_in = 0.0
+    times, iters = [], []
+    budget = args.cpu_budget
+    t_start = time.perf_counter()
+    while True:
+        inv = orc.cfl()
+        dt, t_in = fsim_dt(inv, t_in)
+        t0 = time.perf_counter()
+        st = orc.step(dt, mode=1, precision=0, max_iterations=args.max_iterations, tol=args.tol)
+        times.append(time.perf_counter() - t0)
+        iters.append(st.iterations)
+        if time.perf_counter() - t_start > budget or len(times) >= args.cpu_steps:
+            break
+    return times, iters, orc.particle_count()
+
+
+def fsim_dt(inv, t_in):
+    from oracle.oracle import compute_dt
+
+    dt, t = compute_dt(inv, 1, FRAME_STEP, t_in)
+    if t + 1e-5 >= FRAME_STEP:
+        t = 0.0
+    return dt, t
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dam_break_256", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "fp64"])
+    ap.add_argument("--tol", type=float, default=1e-5)
+    ap.add_argument("--max-iterations", type=int, default=1500)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    wl = WORKLOADS[args.workload]
+    config = {"workload": args.workload, "grid": wl["n"], "scene": wl["scene"],
+              "pcg": f"jacobi {args.precision} relative {args.tol:g} max {args.max_iterations}",
+              "cfl": 1, "flip": 0.95, "frame_rate": 30,
+              "l2": "inputs larger than L2 (particle state > 129 MB)",
+              "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # Each step is one full reference FLIP step (~tens of seconds at
+        # 256^3); the run is capped at 1 warm-up + 2 timed steps so that it
+        # ends within a few minutes.
+        args.cpu_steps = 1 + min(args.steps, 2) if args.warmup > 0 else min(args.steps, 2)
+        args.cpu_budget = 1e9
+        times, iters, npart = cpu_sample(args)
+        timed = times[1:] if args.warmup > 0 and len(times) > 1 else times
+        v = len(timed) / sum(timed)
+        line = {"impl": "reference", "metric": "FLIP steps/s", "value": v, "unit": "steps/s",
+                "n_gpus": args.gpus, "steps": len(timed), "warmup": len(times) - len(timed),
+                "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                                 "sample": f"{len(timed)} full steps of {args.workload} "
+                                           f"({npart} particles, PCG iters {iters})"},
+                "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    res = run_gpu(args, rank, world)
+    if rank != 0:
+        return
+    value = world * args.steps / (res["ms"] * 1e-3)
+    line = {"metric": "FLIP steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": dict(config, particles=res["n_particles"],
+                                                 fluid_cells=res["n_fluid"],
+                                                 pcg_iters_per_step=float(np.mean(res["iters"]))),
+            "roofline": roofline(res),
+            "e2e": {"value": 1e3 / res["e2e_ms"], "unit": "steps/s",
+                    "h2d_bytes_per_step": res["e2e_bytes"], "d2h_bytes_per_step": res["e2e_bytes"]},
+            "gpu_launches": res["launches"], "clocks": res["clocks"],
+            "kernels_ms": {k: round(v[0], 3) for k, v in sorted(res["kt"].items(),
+                                                                key=lambda kv: -kv[1][0])}}
+    if not args.no_cpu:
+        times, iters, npart = cpu_sample(args)
+        v = len(times) / sum(times)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": f"first {len(times)} step(s) of {args.workload} from "
+                                          f"rest ({npart} particles, PCG iters {iters})"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,663 @@
+// k_grid.cu -- grid stages of the FLIP step on the sparse 8^3 brick layout.
+//
+// P2G (FlipSimulation::TransferParticlesToGrid, common/flip_simulation.cc:
+// 809-923, with ScatterWeight<D> :927-1009) runs one CTA per grid leaf.  The
+// CTA walks the 10^3 cells whose particles can reach its 8^3 nodes (the same
+// halo the reference buffers per leaf), splats every particle's trilinear
+// MAC weights into shared-memory accumulators for the nodes it owns, and
+// then writes each node exactly once: no global atomics, no halo write-back.
+// The fused variant folds the rest of the per-node work of the step into
+// that write: normalisation with the 1e-5 cut, ApplyBoundaryConditions,
+// SaveGridVelocities, AddGravity and the second ApplyBoundaryConditions.
+//
+// The remaining kernels restate ComputeDivergence (:716-736),
+// UpdateVelocityFromPressure (:739-778) fused with GetVelocityUpdate
+// (:781-801) and the CFL max (:460-488), and the per-stage variants.
+// All arithmetic that the reference does in float is done with explicit
+// round-to-nearest intrinsics so that nvcc cannot contract it into FMAs.
+#include <cstring>
+
+#include "fsim_internal.cuh"
+
+namespace fsim {
+
+namespace {
+
+struct GridArgs {
+  const float* part;
+  int64_t cap;
+  const uint32_t* keys;
+  const int32_t* leaf_id;
+  const int32_t* nbr;
+  const uint2* cell_range;
+  const uint2* leaf_range;
+  int n_pleaf, n_gleaf;
+  int check_dead;
+  LeafMap lm;
+  SolidDesc sd;
+  float* vel;
+  float* vold;
+  float* weight;
+  uint32_t* vel_on;
+  uint32_t* vold_on;
+  int8_t* marker;
+  const float* pres;
+  float* div;
+  float dt, fx, fy, fz;
+  int64_t* cnt;
+};
+
+__device__ __forceinline__ void origin_of(const GridArgs& a, int s, int o[3]) {
+  int lx, ly, lz;
+  leaf_coords(a.lm, uint32_t(a.leaf_id[s]), lx, ly, lz);
+  o[0] = lx * 8; o[1] = ly * 8; o[2] = lz * 8;
+}
+
+__device__ __forceinline__ int nb_index(int dx, int dy, int dz) {
+  return (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1);
+}
+
+// neighbour-leaf direction of local coordinate t in [-1, 8]
+__device__ __forceinline__ int side(int t) { return t < 0 ? -1 : (t > 7 ? 1 : 0); }
+
+__device__ __forceinline__ bool in_box(const int n[3], int i, int j, int k) {
+  return i >= 0 && j >= 0 && k >= 0 && i < n[0] && j < n[1] && k < n[2];
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a) {
+  __shared__ float sv[3][512];
+  __shared__ float sw[3][512];
+  __shared__ uint8_t touched[512];
+  __shared__ int nb[27];
+  const int s = blockIdx.x;
+  const int tid = threadIdx.x;
+  int org[3];
+  origin_of(a, s, org);
+  if (tid < 27) nb[tid] = a.nbr[int64_t(s) * 27 + tid];
+  for (int v = tid; v < 512; v += 256) {
+    sv[0][v] = 0.f; sv[1][v] = 0.f; sv[2][v] = 0.f;
+    sw[0][v] = 0.f; sw[1][v] = 0.f; sw[2][v] = 0.f;
+    touched[v] = 0;
+  }
+  __syncthreads();
+  const float* px = a.part;
+  const int64_t cap = a.cap;
+  for (int c = tid; c < 1000; c += 256) {
+    const int ci = c / 100 - 1, cj = (c / 10) % 10 - 1, ck = c % 10 - 1;  // local [-1,8]
+    const int ns = nb[nb_index(side(ci), side(cj), side(ck))];
+    if (ns < 0 || ns >= a.n_pleaf) continue;
+    const int g[3] = {org[0] + ci, org[1] + cj, org[2] + ck};
+    const int vox = ((g[0] & 7) << 6) | ((g[1] & 7) << 3) | (g[2] & 7);
+    const uint2 rg = a.cell_range[int64_t(ns) * 512 + vox];
+    for (uint32_t q = rg.x; q < rg.y; ++q) {
+      if (a.check_dead && a.keys[q] == kDeadKey) continue;
+      const float p[3] = {px[q], px[cap + q], px[2 * cap + q]};
+      const float u[3] = {px[3 * cap + q], px[4 * cap + q], px[5 * cap + q]};
+#pragma unroll
+      for (int D = 0; D < 3; ++D) {
+        float lo[3] = {float(g[0]), float(g[1]), float(g[2])};
+        int st[3] = {g[0], g[1], g[2]};
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          if (ax == D) continue;
+          lo[ax] = __fadd_rn(lo[ax], 0.5f);
+          if (p[ax] < lo[ax]) { lo[ax] = __fsub_rn(lo[ax], 1.0f); st[ax] -= 1; }
+        }
+        const float x = __fsub_rn(p[0], lo[0]), y = __fsub_rn(p[1], lo[1]),
+                    z = __fsub_rn(p[2], lo[2]);
+        const float xy = __fmul_rn(x, y), yz = __fmul_rn(y, z), xz = __fmul_rn(z, x),
+                    xyz = __fmul_rn(xy, z);
+        float w[2][2][2];
+        w[1][1][1] = xyz;
+        w[1][1][0] = __fsub_rn(xy, xyz);
+        w[1][0][1] = __fsub_rn(xz, xyz);
+        w[1][0][0] = __fsub_rn(__fsub_rn(x, xz), w[1][1][0]);
+        w[0][1][1] = __fsub_rn(yz, xyz);
+        w[0][1][0] = __fsub_rn(__fsub_rn(y, yz), w[1][1][0]);
+        w[0][0][1] = __fsub_rn(__fsub_rn(z, yz), w[1][0][1]);
+        w[0][0][0] = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(1.0f, x), y), xy), w[0][0][1]);
+        const int l0 = st[0] - org[0], l1 = st[1] - org[1], l2 = st[2] - org[2];
+#pragma unroll
+        for (int di = 0; di < 2; ++di)
+#pragma unroll
+          for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+              const int i = l0 + di, j = l1 + dj, k = l2 + dk;
+              if ((unsigned)i < 8u && (unsigned)j < 8u && (unsigned)k < 8u) {
+                const int o = (i << 6) | (j << 3) | k;
+                const float ww = w[di][dj][dk];
+                atomicAdd(&sv[D][o], __fmul_rn(ww, u[D]));
+                atomicAdd(&sw[D][o], ww);
+                touched[o] = 1;
+              }
+            }
+      }
+    }
+  }
+  __syncthreads();
+  float* vel = a.vel + int64_t(s) * 1536;
+  for (int v = tid; v < 512; v += 256) {
+    const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
+    const int g[3] = {org[0] + x, org[1] + y, org[2] + z};
+    const bool on = touched[v] != 0;
+    float val[3];
+#pragma unroll
+    for (int D = 0; D < 3; ++D) {
+      const float ws = sw[D][v];
+      // THRESH is a double literal in the reference: float ws < 1e-5 (double)
+      // is ws <= 1e-5f
+      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(sv[D][v], ws)) : 0.f;
+    }
+    // marker: FLUID for in-box cells holding particles
+    bool has = false;
+    if (s < a.n_pleaf) {
+      const uint2 rg = a.cell_range[int64_t(s) * 512 + v];
+      has = rg.y > rg.x;
+    }
+    int m = (has && in_box(a.lm.n, g[0], g[1], g[2])) ? FSIM_FLUID : FSIM_AIR;
+    const unsigned ball = __ballot_sync(0xffffffffu, on);
+    if (FUSED) {
+      const bool sc = is_solid(a.sd, g[0], g[1], g[2]);
+      if (sc) m = FSIM_SOLID;
+      bool zero[3];
+      zero[0] = sc != is_solid(a.sd, g[0] - 1, g[1], g[2]);
+      zero[1] = sc != is_solid(a.sd, g[0], g[1] - 1, g[2]);
+      zero[2] = sc != is_solid(a.sd, g[0], g[1], g[2] - 1);
+      float* vold = a.vold + int64_t(s) * 1536;
+      const float gf[3] = {__fmul_rn(a.dt, a.fx), __fmul_rn(a.dt, a.fy), __fmul_rn(a.dt, a.fz)};
+#pragma unroll
+      for (int D = 0; D < 3; ++D) {
+        float vv = val[D];
+        if (on && zero[D]) vv = 0.f;                 // ApplyBoundaryConditions
+        vold[D * 512 + v] = vv;                      // SaveGridVelocities
+        if (on) vv = (D == 1) ? __fsub_rn(vv, gf[1]) : __fadd_rn(vv, gf[D]);  // AddGravity
+        if (on && zero[D]) vv = 0.f;                 // ApplyBoundaryConditions
+        vel[D * 512 + v] = vv;
+      }
+      if ((threadIdx.x & 31) == 0) {
+        a.vold_on[int64_t(s) * 16 + (v >> 5)] = ball;
+      }
+    } else {
+      float* wt = a.weight + int64_t(s) * 1536;
+#pragma unroll
+      for (int D = 0; D < 3; ++D) {
+        vel[D * 512 + v] = val[D];
+        wt[D * 512 + v] = on ? sw[D][v] : 0.f;
+      }
+      // ClearGridData left the saved velocity empty
+      if ((threadIdx.x & 31) == 0) a.vold_on[int64_t(s) * 16 + (v >> 5)] = 0u;
+    }
+    if ((threadIdx.x & 31) == 0) a.vel_on[int64_t(s) * 16 + (v >> 5)] = ball;
+    a.marker[int64_t(s) * 512 + v] = int8_t(m);
+  }
+}
+
+__device__ __forceinline__ bool bit_on(const uint32_t* bits, int s, int v) {
+  return (bits[int64_t(s) * 16 + (v >> 5)] >> (v & 31)) & 1u;
+}
+
+// ApplyBoundaryConditions (per-stage): marker SOLID on solid cells, normal
+// component zeroed on active faces with solid on exactly one side.
+__global__ void __launch_bounds__(256) k_apply_bc(const __grid_constant__ GridArgs a) {
+  const int s = blockIdx.x;
+  int org[3];
+  origin_of(a, s, org);
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    const int g[3] = {org[0] + (v >> 6), org[1] + ((v >> 3) & 7), org[2] + (v & 7)};
+    const bool sc = is_solid(a.sd, g[0], g[1], g[2]);
+    if (sc) a.marker[int64_t(s) * 512 + v] = FSIM_SOLID;
+    if (!bit_on(a.vel_on, s, v)) continue;
+    float* vel = a.vel + int64_t(s) * 1536;
+    if (sc != is_solid(a.sd, g[0] - 1, g[1], g[2])) vel[v] = 0.f;
+    if (sc != is_solid(a.sd, g[0], g[1] - 1, g[2])) vel[512 + v] = 0.f;
+    if (sc != is_solid(a.sd, g[0], g[1], g[2] - 1)) vel[1024 + v] = 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_save(const __grid_constant__ GridArgs a) {
+  const int s = blockIdx.x;
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    const bool on = bit_on(a.vel_on, s, v);
+#pragma unroll
+    for (int D = 0; D < 3; ++D)
+      a.vold[int64_t(s) * 1536 + D * 512 + v] = on ? a.vel[int64_t(s) * 1536 + D * 512 + v] : 0.f;
+    if (v < 16) a.vold_on[int64_t(s) * 16 + v] = a.vel_on[int64_t(s) * 16 + v];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_gravity(const __grid_constant__ GridArgs a) {
+  const int s = blockIdx.x;
+  const float gf[3] = {__fmul_rn(a.dt, a.fx), __fmul_rn(a.dt, a.fy), __fmul_rn(a.dt, a.fz)};
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    if (!bit_on(a.vel_on, s, v)) continue;
+    float* vel = a.vel + int64_t(s) * 1536;
+    vel[v] = __fadd_rn(vel[v], gf[0]);
+    vel[512 + v] = __fsub_rn(vel[512 + v], gf[1]);
+    vel[1024 + v] = __fadd_rn(vel[1024 + v], gf[2]);
+  }
+}
+
+// Particles::DeleteOutsideParticles: particles whose cell is outside the box
+// get the dead key (they stop contributing and are dropped at the next sort).
+__global__ void k_delete_outside(uint32_t* __restrict__ keys, int64_t n, LeafMap lm,
+                                 int64_t* __restrict__ ndead) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = keys[i];
+  if (k == kDeadKey) return;
+  int lx, ly, lz;
+  leaf_coords(lm, k >> 9, lx, ly, lz);
+  const int v = int(k & 511u);
+  const int c0 = lx * 8 + (v >> 6), c1 = ly * 8 + ((v >> 3) & 7), c2 = lz * 8 + (v & 7);
+  if (!in_box(lm.n, c0, c1, c2)) {
+    keys[i] = kDeadKey;
+    atomicAdd(reinterpret_cast<unsigned long long*>(ndead), 1ull);
+  }
+}
+
+// velocity component D at global node g, from leaf slot s's neighbourhood
+__device__ __forceinline__ float vel_at(const GridArgs& a, const float* field, const int* nb,
+                                        const int org[3], int D, int gx, int gy, int gz) {
+  const int lx = gx - org[0], ly = gy - org[1], lz = gz - org[2];
+  const int ns = nb[nb_index(side(lx), side(ly), side(lz))];
+  if (ns < 0) return 0.f;
+  const int v = ((gx & 7) << 6) | ((gy & 7) << 3) | (gz & 7);
+  return field[int64_t(ns) * 1536 + D * 512 + v];
+}
+
+__device__ __forceinline__ int marker_at(const GridArgs& a, const int* nb, const int org[3],
+                                         int gx, int gy, int gz) {
+  const int lx = gx - org[0], ly = gy - org[1], lz = gz - org[2];
+  const int ns = nb[nb_index(side(lx), side(ly), side(lz))];
+  if (ns < 0) return FSIM_AIR;
+  const int v = ((gx & 7) << 6) | ((gy & 7) << 3) | (gz & 7);
+  return a.marker[int64_t(ns) * 512 + v];
+}
+
+__device__ __forceinline__ float pres_at(const GridArgs& a, const int* nb, const int org[3],
+                                         int gx, int gy, int gz) {
+  const int lx = gx - org[0], ly = gy - org[1], lz = gz - org[2];
+  const int ns = nb[nb_index(side(lx), side(ly), side(lz))];
+  if (ns < 0 || ns >= a.n_pleaf) return 0.f;
+  const int v = ((gx & 7) << 6) | ((gy & 7) << 3) | (gz & 7);
+  return a.pres[int64_t(ns) * 512 + v];
+}
+
+// ComputeDivergence over particle leaves (FLUID cells only live there).
+__global__ void __launch_bounds__(256) k_divergence(const __grid_constant__ GridArgs a) {
+  __shared__ int nb[27];
+  const int s = blockIdx.x;
+  if (threadIdx.x < 27) nb[threadIdx.x] = a.nbr[int64_t(s) * 27 + threadIdx.x];
+  int org[3];
+  origin_of(a, s, org);
+  __syncthreads();
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    const int g[3] = {org[0] + (v >> 6), org[1] + ((v >> 3) & 7), org[2] + (v & 7)};
+    float d = 0.f;
+    if (a.marker[int64_t(s) * 512 + v] == FSIM_FLUID) {
+      const float* vel = a.vel + int64_t(s) * 1536;
+      d = __fsub_rn(vel_at(a, a.vel, nb, org, 0, g[0] + 1, g[1], g[2]), vel[v]);
+      d = __fadd_rn(d, __fsub_rn(vel_at(a, a.vel, nb, org, 1, g[0], g[1] + 1, g[2]), vel[512 + v]));
+      d = __fadd_rn(d, __fsub_rn(vel_at(a, a.vel, nb, org, 2, g[0], g[1], g[2] + 1), vel[1024 + v]));
+    }
+    a.div[int64_t(s) * 512 + v] = d;
+  }
+}
+
+__device__ __forceinline__ void atomic_max_pos(int64_t* cnt, float v) {
+  // non-negative floats order like their bit patterns
+  atomicMax(reinterpret_cast<unsigned long long*>(cnt), (unsigned long long)__float_as_uint(v));
+}
+
+// UpdateVelocityFromPressure over faces [0,N]^3; FUSED also forms
+// GetVelocityUpdate (v_old := v - v_old on active faces) and the CFL max.
+template <bool FUSED>
+__global__ void __launch_bounds__(256) k_pressure_update(const __grid_constant__ GridArgs a) {
+  __shared__ int nb[27];
+  __shared__ float red[8];
+  const int s = blockIdx.x;
+  if (threadIdx.x < 27) nb[threadIdx.x] = a.nbr[int64_t(s) * 27 + threadIdx.x];
+  int org[3];
+  origin_of(a, s, org);
+  __syncthreads();
+  const int* n = a.lm.n;
+  float vmax = 0.f;
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    const int g[3] = {org[0] + (v >> 6), org[1] + ((v >> 3) & 7), org[2] + (v & 7)};
+    if (g[0] < 0 || g[1] < 0 || g[2] < 0 || g[0] > n[0] || g[1] > n[1] || g[2] > n[2]) continue;
+    float* vel = a.vel + int64_t(s) * 1536;
+    const int mc = a.marker[int64_t(s) * 512 + v];
+    bool on = bit_on(a.vel_on, s, v);
+    float val[3] = {vel[v], vel[512 + v], vel[1024 + v]};
+    if (mc != FSIM_SOLID) {
+      const float pc = (s < a.n_pleaf) ? a.pres[int64_t(s) * 512 + v] : 0.f;
+      bool upd = false;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int h0 = g[0] - (d == 0), h1 = g[1] - (d == 1), h2 = g[2] - (d == 2);
+        const int mn = marker_at(a, nb, org, h0, h1, h2);
+        if ((mn == FSIM_FLUID || mc == FSIM_FLUID) && mn != FSIM_SOLID) {
+          val[d] = __fadd_rn(val[d], __fsub_rn(pc, pres_at(a, nb, org, h0, h1, h2)));
+          upd = true;
+        }
+      }
+      if (upd) {
+        vel[v] = val[0]; vel[512 + v] = val[1]; vel[1024 + v] = val[2];
+        if (!on) {
+          atomicOr(&a.vel_on[int64_t(s) * 16 + (v >> 5)], 1u << (v & 31));
+          on = true;
+        }
+      }
+    }
+    if (FUSED && on) {
+      float* vold = a.vold + int64_t(s) * 1536;
+#pragma unroll
+      for (int D = 0; D < 3; ++D) vold[D * 512 + v] = __fsub_rn(val[D], vold[D * 512 + v]);
+      if (g[0] < n[0] && g[1] < n[1] && g[2] < n[2]) {
+        if (g[1] != n[1] - 1 && g[2] != n[2] - 1) vmax = fmaxf(vmax, fabsf(val[0]));
+        if (g[0] != n[0] - 1 && g[2] != n[2] - 1) vmax = fmaxf(vmax, fabsf(val[1]));
+        if (g[0] != n[0] - 1 && g[1] != n[1] - 1) vmax = fmaxf(vmax, fabsf(val[2]));
+      }
+    }
+  }
+  if (FUSED) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float m = 0.f;
+      for (int w = 0; w < 8; ++w) m = fmaxf(m, red[w]);
+      if (m > 0.f) atomic_max_pos(a.cnt + 4, m);
+    }
+  }
+}
+
+// GetVelocityUpdate (per-stage) over faces [0,N]^3.
+__global__ void __launch_bounds__(256) k_velocity_update(const __grid_constant__ GridArgs a) {
+  const int s = blockIdx.x;
+  int org[3];
+  origin_of(a, s, org);
+  const int* n = a.lm.n;
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    const int g[3] = {org[0] + (v >> 6), org[1] + ((v >> 3) & 7), org[2] + (v & 7)};
+    if (g[0] < 0 || g[1] < 0 || g[2] < 0 || g[0] > n[0] || g[1] > n[1] || g[2] > n[2]) continue;
+    const bool on = bit_on(a.vel_on, s, v), oo = bit_on(a.vold_on, s, v);
+    if (on && !oo) atomicAdd(reinterpret_cast<unsigned long long*>(a.cnt + 3), 1ull);
+    if (on && oo) {
+      float* vel = a.vel + int64_t(s) * 1536;
+      float* vold = a.vold + int64_t(s) * 1536;
+#pragma unroll
+      for (int D = 0; D < 3; ++D) vold[D * 512 + v] = __fsub_rn(vel[D * 512 + v], vold[D * 512 + v]);
+    }
+  }
+}
+
+// CFL max over active in-box faces (FlipSimulation::CFL).
+__global__ void __launch_bounds__(256) k_cfl(const __grid_constant__ GridArgs a) {
+  __shared__ float red[8];
+  const int s = blockIdx.x;
+  int org[3];
+  origin_of(a, s, org);
+  const int* n = a.lm.n;
+  float vmax = 0.f;
+  for (int v = threadIdx.x; v < 512; v += 256) {
+    const int g[3] = {org[0] + (v >> 6), org[1] + ((v >> 3) & 7), org[2] + (v & 7)};
+    if (!in_box(n, g[0], g[1], g[2]) || !bit_on(a.vel_on, s, v)) continue;
+    const float* vel = a.vel + int64_t(s) * 1536;
+    if (g[1] != n[1] - 1 && g[2] != n[2] - 1) vmax = fmaxf(vmax, fabsf(vel[v]));
+    if (g[0] != n[0] - 1 && g[2] != n[2] - 1) vmax = fmaxf(vmax, fabsf(vel[512 + v]));
+    if (g[0] != n[0] - 1 && g[1] != n[1] - 1) vmax = fmaxf(vmax, fabsf(vel[1024 + v]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = vmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int w = 0; w < 8; ++w) m = fmaxf(m, red[w]);
+    if (m > 0.f) atomic_max_pos(a.cnt + 4, m);
+  }
+}
+
+// ---- dense downloads ------------------------------------------------------
+struct DenseArgs {
+  LeafMap lm;
+  SolidDesc sd;
+  const int32_t* slot;  // dense leaf id -> slot
+  int n_pleaf;
+  const float* vec;     // slot*1536 (Vec3 fields)
+  const uint32_t* on;   // slot*16
+  const float* sca;     // pleaf*512 (scalar fields)
+  const int8_t* marker;
+  int field;            // FSIM_FIELD_* or 100 marker
+  int valid, extrap, bc;
+  float* out;
+  int32_t* iout;
+  uint8_t* act;
+};
+
+__device__ __forceinline__ int slot_of(const DenseArgs& a, int i, int j, int k) {
+  const int lx = fdiv(i, 8), ly = fdiv(j, 8), lz = fdiv(k, 8);
+  if (!leaf_valid(a.lm, lx, ly, lz)) return -1;
+  return a.slot[leaf_id(a.lm, lx, ly, lz)];
+}
+
+__global__ void k_dense(const __grid_constant__ DenseArgs a) {
+  const int* n = a.lm.n;
+  const int64_t s1 = n[1] + 2, s2 = n[2] + 2;
+  const int64_t tot = int64_t(n[0] + 2) * s1 * s2;
+  int64_t o = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (o >= tot) return;
+  const int i = int(o / (s1 * s2)) - 1, j = int((o / s2) % s1) - 1, k = int(o % s2) - 1;
+  const int vox = ((i & 7) << 6) | ((j & 7) << 3) | (k & 7);
+  const int sl = slot_of(a, i, j, k);
+  if (a.field == 100) {  // marker
+    int m = 0;
+    if (a.valid && sl >= 0) m = a.marker[int64_t(sl) * 512 + vox];
+    if (a.bc && is_solid(a.sd, i, j, k)) m = FSIM_SOLID;
+    a.iout[o] = m;
+    if (a.act) a.act[o] = m != 0;
+    return;
+  }
+  if (a.field <= FSIM_FIELD_WEIGHT) {
+    bool on = a.valid && sl >= 0 && ((a.on[int64_t(sl) * 16 + (vox >> 5)] >> (vox & 31)) & 1u);
+    const int c[3] = {i, j, k};
+    for (int D = 0; D < 3; ++D) {
+      float val = 0.f;
+      if (a.valid) {
+        int src[3] = {i, j, k};
+        if (a.extrap && a.field != FSIM_FIELD_WEIGHT) ghost_source(n, D, c, src);
+        const int ss = slot_of(a, src[0], src[1], src[2]);
+        if (ss >= 0) {
+          const int sv = ((src[0] & 7) << 6) | ((src[1] & 7) << 3) | (src[2] & 7);
+          const bool son = (a.on[int64_t(ss) * 16 + (sv >> 5)] >> (sv & 31)) & 1u;
+          if (son) val = a.vec[int64_t(ss) * 1536 + D * 512 + sv];
+        }
+      }
+      a.out[3 * o + D] = val;
+    }
+    if (a.extrap && a.field != FSIM_FIELD_WEIGHT && extrap_activated(n, i, j, k)) on = true;
+    if (a.act) a.act[o] = on;
+    if (!on) { a.out[3 * o] = 0.f; a.out[3 * o + 1] = 0.f; a.out[3 * o + 2] = 0.f; }
+    return;
+  }
+  // scalar fields on FLUID cells (div, pressure, phi)
+  bool fl = false;
+  if (a.valid && sl >= 0) fl = a.marker[int64_t(sl) * 512 + vox] == FSIM_FLUID;
+  float val = (a.field == FSIM_FIELD_PHI) ? 5.0f : 0.f;
+  if (fl) {
+    if (a.field == FSIM_FIELD_PHI) val = -0.5f;
+    else if (sl < a.n_pleaf) val = a.sca[int64_t(sl) * 512 + vox];
+  }
+  a.out[o] = val;
+  if (a.act) a.act[o] = fl;
+}
+
+inline unsigned nblk(int64_t n, int b) { return unsigned((n + b - 1) / b); }
+
+GridArgs make_args(fsim_sim* s) {
+  GridArgs a;
+  a.part = s->part[s->cur];
+  a.cap = s->cap_p;
+  a.keys = s->keys[0];
+  a.leaf_id = s->d_leaf_id;
+  a.nbr = s->d_nbr;
+  a.cell_range = s->d_cell_range;
+  a.leaf_range = s->d_leaf_range;
+  a.n_pleaf = s->n_pleaf;
+  a.n_gleaf = s->n_gleaf;
+  a.check_dead = s->deleted_outside ? 1 : 0;
+  a.lm = s->lm;
+  a.sd = s->solid;
+  a.vel = s->vel;
+  a.vold = s->vold;
+  a.weight = s->weight;
+  a.vel_on = s->vel_on;
+  a.vold_on = s->vold_on;
+  a.marker = s->marker;
+  a.pres = s->pres;
+  a.div = s->div;
+  a.dt = 0.f;
+  a.fx = s->cfg.force[0];
+  a.fy = s->cfg.force[1];
+  a.fz = s->cfg.force[2];
+  a.cnt = s->d_cnt;
+  return a;
+}
+
+}  // namespace
+
+int launch_p2g(fsim_sim* s, bool fused, float dt) {
+  GridArgs a = make_args(s);
+  a.dt = dt;
+  if (fused)
+    FSIM_LAUNCH(s, "p2g_fused", k_p2g<true>, s->n_gleaf, 256, 0, a);
+  else
+    FSIM_LAUNCH(s, "p2g", k_p2g<false>, s->n_gleaf, 256, 0, a);
+  return FSIM_OK;
+}
+
+int launch_apply_bc(fsim_sim* s) {
+  FSIM_LAUNCH(s, "apply_bc", k_apply_bc, s->n_gleaf, 256, 0, make_args(s));
+  return FSIM_OK;
+}
+
+int launch_save_velocities(fsim_sim* s) {
+  FSIM_LAUNCH(s, "save_velocities", k_save, s->n_gleaf, 256, 0, make_args(s));
+  return FSIM_OK;
+}
+
+int launch_add_gravity(fsim_sim* s, float dt) {
+  GridArgs a = make_args(s);
+  a.dt = dt;
+  FSIM_LAUNCH(s, "add_gravity", k_gravity, s->n_gleaf, 256, 0, a);
+  return FSIM_OK;
+}
+
+int launch_delete_outside(fsim_sim* s) {
+  FSIM_LAUNCH(s, "delete_outside", k_delete_outside, nblk(s->n_live, 256), 256, 0, s->keys[0],
+              s->n_live, s->lm, s->d_cnt + 6);
+  return FSIM_OK;
+}
+
+int launch_divergence(fsim_sim* s) {
+  FSIM_LAUNCH(s, "divergence", k_divergence, s->n_pleaf, 256, 0, make_args(s));
+  return FSIM_OK;
+}
+
+int launch_pressure_update(fsim_sim* s, bool fused) {
+  if (fused) {
+    FSIM_CK(s, cudaMemsetAsync(s->d_cnt + 4, 0, sizeof(int64_t), s->stream));
+    FSIM_LAUNCH(s, "pressure_update_fused", k_pressure_update<true>, s->n_gleaf, 256, 0,
+                make_args(s));
+  } else {
+    FSIM_LAUNCH(s, "pressure_update", k_pressure_update<false>, s->n_gleaf, 256, 0, make_args(s));
+  }
+  return FSIM_OK;
+}
+
+int launch_velocity_update(fsim_sim* s) {
+  FSIM_CK(s, cudaMemsetAsync(s->d_cnt + 3, 0, sizeof(int64_t), s->stream));
+  FSIM_LAUNCH(s, "velocity_update", k_velocity_update, s->n_gleaf, 256, 0, make_args(s));
+  return FSIM_OK;
+}
+
+int launch_cfl(fsim_sim* s) {
+  FSIM_CK(s, cudaMemsetAsync(s->d_cnt + 4, 0, sizeof(int64_t), s->stream));
+  FSIM_LAUNCH(s, "cfl_max", k_cfl, s->n_gleaf, 256, 0, make_args(s));
+  return FSIM_OK;
+}
+
+static int ensure_dense(fsim_sim* s, size_t bytes) {
+  if (s->dense_tmp.bytes >= bytes) return FSIM_OK;
+  if (s->dense_tmp.p) cudaFree(s->dense_tmp.p);
+  s->dense_tmp.p = nullptr;
+  s->dense_tmp.bytes = 0;
+  FSIM_CK(s, cudaMalloc(&s->dense_tmp.p, bytes));
+  s->dense_tmp.bytes = bytes;
+  return FSIM_OK;
+}
+
+static DenseArgs dense_args(fsim_sim* s) {
+  DenseArgs a;
+  memset(&a, 0, sizeof(a));
+  a.lm = s->lm;
+  a.sd = s->solid;
+  a.slot = s->d_slot;
+  a.n_pleaf = s->n_pleaf;
+  a.marker = s->marker;
+  return a;
+}
+
+int download_dense(fsim_sim* s, int field, float* out, uint8_t* active) {
+  const int* n = s->lm.n;
+  const int64_t tot = int64_t(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  const int comps = (field <= FSIM_FIELD_WEIGHT) ? 3 : 1;
+  const size_t fb = size_t(tot) * comps * sizeof(float);
+  int rc = ensure_dense(s, fb + size_t(tot));
+  if (rc) return rc;
+  DenseArgs a = dense_args(s);
+  a.field = field;
+  a.out = static_cast<float*>(s->dense_tmp.p);
+  a.act = static_cast<uint8_t*>(s->dense_tmp.p) + fb;
+  bool have = s->have_topology && s->grid_valid;
+  switch (field) {
+    case FSIM_FIELD_VELOCITY: a.vec = s->vel; a.on = s->vel_on; a.valid = have; a.extrap = s->extrapolated; break;
+    case FSIM_FIELD_VELOCITY_UPDATE: a.vec = s->vold; a.on = s->vold_on; a.valid = have && s->saved; a.extrap = s->extrapolated; break;
+    case FSIM_FIELD_WEIGHT: a.vec = s->weight; a.on = s->vel_on; a.valid = have && s->weight_valid; break;
+    case FSIM_FIELD_DIVERGENCE: a.sca = s->div; a.valid = have && s->div_valid; break;
+    case FSIM_FIELD_PRESSURE: a.sca = s->pres; a.valid = have && s->pres_valid; break;
+    case FSIM_FIELD_PHI: a.valid = have && s->phi_valid; break;
+    default: return fail(s, FSIM_ERR_INVALID, "unknown field");
+  }
+  FSIM_LAUNCH(s, "dense_download", k_dense, nblk(tot, 256), 256, 0, a);
+  FSIM_CK(s, cudaMemcpyAsync(out, a.out, fb, cudaMemcpyDeviceToHost, s->stream));
+  if (active)
+    FSIM_CK(s, cudaMemcpyAsync(active, a.act, size_t(tot), cudaMemcpyDeviceToHost, s->stream));
+  FSIM_CK(s, cudaStreamSynchronize(s->stream));
+  return FSIM_OK;
+}
+
+int download_marker(fsim_sim* s, int32_t* out, uint8_t* active) {
+  const int* n = s->lm.n;
+  const int64_t tot = int64_t(n[0] + 2) * (n[1] + 2) * (n[2] + 2);
+  int rc = ensure_dense(s, size_t(tot) * 5);
+  if (rc) return rc;
+  DenseArgs a = dense_args(s);
+  a.field = 100;
+  a.iout = static_cast<int32_t*>(s->dense_tmp.p);
+  a.act = static_cast<uint8_t*>(s->dense_tmp.p) + size_t(tot) * 4;
+  a.valid = s->have_topology && s->grid_valid;
+  a.bc = s->bc_applied;
+  FSIM_LAUNCH(s, "dense_download", k_dense, nblk(tot, 256), 256, 0, a);
+  FSIM_CK(s, cudaMemcpyAsync(out, a.iout, size_t(tot) * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (active)
+    FSIM_CK(s, cudaMemcpyAsync(active, a.act, size_t(tot), cudaMemcpyDeviceToHost, s->stream));
+  FSIM_CK(s, cudaStreamSynchronize(s->stream));
+  return FSIM_OK;
+}
+
+}  // namespace fsim

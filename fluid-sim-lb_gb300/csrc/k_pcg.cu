@@ -1,0 +1,687 @@
+// k_pcg.cu -- Jacobi-preconditioned CG pressure solve on the brick layout.
+//
+// Restates PCGDriver::Solve (common/solver_driver.cc:14-69) with the
+// PCGSolver stages of common/solver.cc: PreparePCGSolver (:263-286),
+// ComputeLocal1 (:297-309), ComputeLocal2 (:324-346), ComputeLocal3
+// (:356-366), the loop test at the head of each iteration (:319-337) and
+// CopySolution (:94-99).  The matrix is never stored: row (i,j,k) of the
+// Laplacian of Solver::CreateLaplacianMatrix (:198-233) is diag = number of
+// non-SOLID neighbours and -1 at each FLUID neighbour, so A*p only needs a
+// per-cell flags byte (bit0 FLUID, bits1-3 diag).  The product is summed in
+// the column order of the reference's sorted sparse rows (-x,-y,-z, diag,
+// +z,+y,+x), which makes it bit-identical to the oracle for identical p.
+//
+// Per iteration two kernels run back to back on device-resident scalars:
+//   spmv:   p_j = z_j + beta_{j-1} p_{j-1} (z = r/diag recomputed, never
+//           stored), p_j.(A p_j); the last CTA forms alpha.
+//   update: A p_j recomputed from p_j (Ap is never stored), x += alpha p,
+//           r -= alpha Ap, r.r and r.z; the last CTA forms beta, counts the
+//           iteration and sets the stop flag.
+// HBM bytes per unknown per iteration: spmv reads r, p_{j-1}, flags and
+// writes p_j (13 B); update reads p_j, x, r, flags and writes x, r (21 B).
+// Each CTA stages one leaf's p plus its six face halos in shared memory;
+// every thread owns one z-quad of 4 cells (float4 / double2 accesses).  Kernels launched after the stop flag is set return at
+// once, so the host polls the flag only between chunks of iterations.
+//
+// Precision modes: FP32 (reference: fp32 vectors, fp32 dots), MIXED (fp32
+// vectors, dots accumulated exactly: FMA error-free products and
+// double-float sums per thread, fp64 above; plus an fp64 outer refinement
+// r = b - A x with x kept in fp64) and FP64 (fp64 vectors and dots).
+#include <algorithm>
+#include <cstring>
+
+#include "fsim_internal.cuh"
+
+namespace fsim {
+
+namespace {
+
+constexpr int kThreads = 128;  // 4 cells per thread, one 8^3 leaf per pass
+
+// Jacobi: T(1.0/diag) (diag 0 gives inf, as 1.0/0 does in the reference)
+__constant__ float c_invf[8] = {__builtin_inff(), 1.0f, 0.5f, float(1.0 / 3.0),
+                                0.25f, float(1.0 / 5.0), float(1.0 / 6.0), float(1.0 / 7.0)};
+__constant__ double c_invd[8] = {__builtin_inf(), 1.0, 0.5, 1.0 / 3.0,
+                                 0.25, 1.0 / 5.0, 1.0 / 6.0, 1.0 / 7.0};
+
+template <typename T>
+__device__ __forceinline__ T inv_diag(uint8_t f);
+template <>
+__device__ __forceinline__ float inv_diag<float>(uint8_t f) {
+  return (f & 1) ? c_invf[flag_diag(f)] : 0.f;
+}
+template <>
+__device__ __forceinline__ double inv_diag<double>(uint8_t f) {
+  return (f & 1) ? c_invd[flag_diag(f)] : 0.0;
+}
+
+__device__ __forceinline__ float tmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float tadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float tsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double tmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double tadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double tsub(double a, double b) { return __dsub_rn(a, b); }
+
+// ---- dot accumulators ----------------------------------------------------
+// DM 0: plain fp32; DM 1: exact products + double-float sum; DM 2: fp64.
+template <int DM>
+struct Dot;
+template <>
+struct Dot<0> {
+  float s = 0.f;
+  __device__ void add(float a, float b) { s = __fadd_rn(s, __fmul_rn(a, b)); }
+  __device__ double value() const { return double(s); }
+};
+template <>
+struct Dot<1> {
+  float hi = 0.f, lo = 0.f;
+  __device__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);  // exact: a*b = p + e
+    const float s = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+  }
+  __device__ double value() const { return double(hi) + double(lo); }
+};
+template <>
+struct Dot<2> {
+  double s = 0.0;
+  __device__ void add(double a, double b) { s = __fma_rn(a, b, s); }
+  __device__ double value() const { return s; }
+};
+
+// Block-level sum of NV values.  DM 0 sums in fp32, otherwise fp64.
+// Result valid in thread 0.
+template <int DM, int NV>
+__device__ void block_sum(double (&v)[NV]) {
+  __shared__ double sh[NV][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    if (DM == 0) {
+      float x = float(v[k]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = __fadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
+      v[k] = double(x);
+    } else {
+      double x = v[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      v[k] = x;
+    }
+    if (lane == 0) sh[k][w] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      if (DM == 0) {
+        float x = 0.f;
+        for (int i = 0; i < kThreads / 32; ++i) x = __fadd_rn(x, float(sh[k][i]));
+        v[k] = double(x);
+      } else {
+        double x = 0.0;
+        for (int i = 0; i < kThreads / 32; ++i) x += sh[k][i];
+        v[k] = x;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Single-pass grid reduction: every block deposits its NV partials; the last
+// block to arrive sums them in a fixed order (deterministic) and returns
+// true in all of its threads with the totals in tot (thread 0).
+template <int DM, int NV>
+__device__ bool grid_sum(double (&v)[NV], double* part, int maxb, unsigned int* counter,
+                         double (&tot)[NV]) {
+  __shared__ bool last;
+  block_sum<DM, NV>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) part[k * maxb + blockIdx.x] = v[k];
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    if (DM == 0) {
+      float x = 0.f;
+      for (int i = threadIdx.x; i < int(gridDim.x); i += kThreads)
+        x = __fadd_rn(x, float(__ldcg(&part[k * maxb + i])));
+      acc[k] = double(x);
+    } else {
+      double x = 0.0;
+      for (int i = threadIdx.x; i < int(gridDim.x); i += kThreads) x += __ldcg(&part[k * maxb + i]);
+      acc[k] = x;
+    }
+  }
+  block_sum<DM, NV>(acc);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) tot[k] = acc[k];
+    *counter = 0u;
+  }
+  return true;
+}
+
+struct PcgArgs {
+  int n_pleaf;
+  int maxb;
+  const int32_t* nbr;
+  const int8_t* marker;
+  const float* b;   // divergence (fp32)
+  uint8_t* flags;
+  void* x;
+  void* r;
+  void* p0;
+  void* p1;
+  void* Ap;
+  double* x64;      // MIXED outer solution
+  float* dinner;    // MIXED inner solution (the fp32 x of the inner solve)
+  PcgScalars* sc;
+  double* part;
+  int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
+};
+
+__device__ __forceinline__ bool converged(const PcgScalars* sc, double rr) {
+  if (sc->mode == FSIM_PCG_FIXED) return false;
+  if (sc->mode == FSIM_PCG_ABSOLUTE) {
+    if (sc->fp32) return float(rr) < float(sc->thr);
+    return rr < sc->thr;
+  }
+  return rr <= sc->thr;
+}
+
+__device__ __forceinline__ double round_t(const PcgScalars* sc, double v) {
+  return sc->fp32 ? double(float(v)) : v;
+}
+
+// Flags from the marker, r = b (or keep), x = 0, and r.r, r.z, b.b.
+template <typename T, int DM>
+__global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ PcgArgs a) {
+  T* x = static_cast<T*>(a.x);
+  T* r = static_cast<T*>(a.r);
+  Dot<DM> drr, drz, dbb;
+  int nfluid = 0;
+  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
+    const int32_t* nb = a.nbr + int64_t(s) * 27;
+    for (int v = threadIdx.x; v < 512; v += kThreads) {
+      const int64_t o = int64_t(s) * 512 + v;
+      const int cx = v >> 6, cy = (v >> 3) & 7, cz = v & 7;
+      uint8_t f = 0;
+      if (a.marker[o] == FSIM_FLUID) {
+        int diag = 0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          int ax = cx, ay = cy, az = cz;
+          const int d = (q & 1) ? 1 : -1;
+          if (q < 2) ax += d; else if (q < 4) ay += d; else az += d;
+          const int sx = ax < 0 ? -1 : (ax > 7 ? 1 : 0), sy = ay < 0 ? -1 : (ay > 7 ? 1 : 0),
+                    sz = az < 0 ? -1 : (az > 7 ? 1 : 0);
+          const int ns = nb[(sx + 1) * 9 + (sy + 1) * 3 + (sz + 1)];
+          int m = FSIM_AIR;
+          if (ns >= 0) m = a.marker[int64_t(ns) * 512 + (((ax & 7) << 6) | ((ay & 7) << 3) | (az & 7))];
+          diag += (m != FSIM_SOLID);
+        }
+        f = uint8_t(1 | (diag << 1));
+        ++nfluid;
+      }
+      a.flags[o] = f;
+      x[o] = T(0);
+      T rv;
+      if (a.init_r) {
+        rv = (f & 1) ? T(a.b[o]) : T(0);
+        r[o] = rv;
+      } else {
+        rv = r[o];
+      }
+      const T z = tmul(inv_diag<T>(f), rv);
+      drr.add(rv, rv);
+      drz.add(rv, z);
+      dbb.add(rv, rv);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nfluid += __shfl_xor_sync(0xffffffffu, nfluid, o);
+  if ((threadIdx.x & 31) == 0 && nfluid)
+    atomicAdd(&a.sc->n_rows, (unsigned long long)nfluid);
+  double v[3] = {drr.value(), drz.value(), dbb.value()};
+  double tot[3];
+  if (grid_sum<DM, 3>(v, a.part, a.maxb, &a.sc->cnt_s, tot) && threadIdx.x == 0) {
+    PcgScalars* sc = a.sc;
+    sc->rr = round_t(sc, tot[0]);
+    sc->rz = round_t(sc, tot[1]);
+    sc->bb = round_t(sc, tot[2]);
+    sc->rr0 = sc->rr;
+    sc->iter = 0;
+    sc->status = FSIM_OK;
+    sc->beta = 0.0;
+    if (sc->mode == FSIM_PCG_RELATIVE) sc->thr = sc->tol2 * sc->bb;
+    sc->done = (sc->max_iter <= 0) || converged(sc, sc->rr);
+  }
+}
+
+// ---- 4-cell vector access: each thread owns cells v0..v0+3 (one z quad)
+template <typename T>
+struct Quad {
+  T v[4];
+};
+__device__ __forceinline__ Quad<float> ld4(const float* p, int64_t o) {
+  const float4 t = *reinterpret_cast<const float4*>(p + o);
+  return Quad<float>{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ Quad<double> ld4(const double* p, int64_t o) {
+  const double2 a = *reinterpret_cast<const double2*>(p + o);
+  const double2 b = *reinterpret_cast<const double2*>(p + o + 2);
+  return Quad<double>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ void st4(float* p, int64_t o, const Quad<float>& q) {
+  *reinterpret_cast<float4*>(p + o) = make_float4(q.v[0], q.v[1], q.v[2], q.v[3]);
+}
+__device__ __forceinline__ void st4(double* p, int64_t o, const Quad<double>& q) {
+  *reinterpret_cast<double2*>(p + o) = make_double2(q.v[0], q.v[1]);
+  *reinterpret_cast<double2*>(p + o + 2) = make_double2(q.v[2], q.v[3]);
+}
+
+// Halo cell h in [0,384): face = h/64 (0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z);
+// returns the neighbour-table index and the voxel inside that neighbour.
+__device__ __forceinline__ void halo_cell(int h, int& q, int& vox) {
+  const int face = h >> 6, u = (h >> 3) & 7, w = h & 7;
+  const int d = (face & 1) ? 1 : -1;
+  const int e = d < 0 ? 7 : 0;
+  if (face < 2) { q = (d + 1) * 9 + 4; vox = (e << 6) | (u << 3) | w; }
+  else if (face < 4) { q = 9 + (d + 1) * 3 + 1; vox = (u << 6) | (e << 3) | w; }
+  else { q = 12 + (d + 1); vox = (u << 6) | (w << 3) | e; }
+}
+
+// A*p for the four cells v0..v0+3 from the staged leaf+halo tile pn, summed
+// in the column order of the reference's rows: -x,-y,-z, diag, +z,+y,+x.
+template <typename T>
+__device__ __forceinline__ void stencil4(const T* pn, int v0, uint32_t f4, T out[4]) {
+  const int cx = v0 >> 6, cy = (v0 >> 3) & 7, cz0 = v0 & 7;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int v = v0 + c, cz = cz0 + c;
+    const uint8_t f = uint8_t(f4 >> (8 * c));
+    T acc = T(0);
+    if (f & 1) {
+      const T mx = cx > 0 ? pn[v - 64] : pn[512 + 0 * 64 + cy * 8 + cz];
+      const T px = cx < 7 ? pn[v + 64] : pn[512 + 1 * 64 + cy * 8 + cz];
+      const T my = cy > 0 ? pn[v - 8] : pn[512 + 2 * 64 + cx * 8 + cz];
+      const T py = cy < 7 ? pn[v + 8] : pn[512 + 3 * 64 + cx * 8 + cz];
+      const T mz = cz > 0 ? pn[v - 1] : pn[512 + 4 * 64 + cx * 8 + cy];
+      const T pz = cz < 7 ? pn[v + 1] : pn[512 + 5 * 64 + cx * 8 + cy];
+      acc = tsub(acc, mx);
+      acc = tsub(acc, my);
+      acc = tsub(acc, mz);
+      acc = tadd(acc, tmul(T(flag_diag(f)), pn[v]));
+      acc = tsub(acc, pz);
+      acc = tsub(acc, py);
+      acc = tsub(acc, px);
+    }
+    out[c] = acc;
+  }
+}
+
+// p_j = z_j + beta_{j-1} p_{j-1} for the leaf and its face halo (z = r/diag
+// recomputed), then p_j.(A p_j); the last CTA forms alpha_j.  Only p_j is
+// written: the update kernel recomputes A p_j from it instead of storing Ap.
+template <typename T, int DM>
+__global__ void __launch_bounds__(kThreads, 12) k_pcg_spmv(const __grid_constant__ PcgArgs a) {
+  __shared__ T pn[512 + 384];
+  const PcgScalars* sc = a.sc;
+  if (sc->done) return;
+  const int it = sc->iter;
+  const T beta = T(sc->beta);
+  const T* r = static_cast<const T*>(a.r);
+  const T* pold = static_cast<const T*>((it & 1) ? a.p0 : a.p1);
+  T* pnew = static_cast<T*>((it & 1) ? a.p1 : a.p0);
+  const uint32_t* flags4 = reinterpret_cast<const uint32_t*>(a.flags);
+  const int v0 = threadIdx.x * 4;
+  Dot<DM> dp;
+  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
+    const int32_t* nb = a.nbr + int64_t(s) * 27;
+    const int64_t o = int64_t(s) * 512 + v0;
+    const uint32_t f4 = flags4[o >> 2];
+    const Quad<T> rq = ld4(r, o);
+    Quad<T> pq;
+    if (it > 0) pq = ld4(pold, o);
+    // halo values first (independent loads in flight)
+    T hv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int h = threadIdx.x + k * kThreads;
+      int q, vox;
+      halo_cell(h, q, vox);
+      const int ns = nb[q];
+      T pv = T(0);
+      if (ns >= 0 && ns < a.n_pleaf) {
+        const int64_t u = int64_t(ns) * 512 + vox;
+        const uint8_t f = a.flags[u];
+        const T z = tmul(inv_diag<T>(f), r[u]);
+        pv = (it == 0) ? z : tadd(z, tmul(beta, pold[u]));
+        if (!(f & 1)) pv = T(0);
+      }
+      hv[k] = pv;
+    }
+    __syncthreads();  // previous leaf's stencil reads of pn are done
+    Quad<T> out;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const uint8_t f = uint8_t(f4 >> (8 * c));
+      T pv = T(0);
+      if (f & 1) {
+        const T z = tmul(inv_diag<T>(f), rq.v[c]);
+        pv = (it == 0) ? z : tadd(z, tmul(beta, pq.v[c]));
+      }
+      out.v[c] = pv;
+      pn[v0 + c] = pv;
+    }
+    st4(pnew, o, out);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pn[512 + threadIdx.x + k * kThreads] = hv[k];
+    __syncthreads();
+    T ap[4];
+    stencil4(pn, v0, f4, ap);
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      if ((f4 >> (8 * c)) & 1u) dp.add(out.v[c], ap[c]);
+  }
+  double v[1] = {dp.value()};
+  double tot[1];
+  if (grid_sum<DM, 1>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
+    PcgScalars* s = a.sc;
+    s->pAp = round_t(s, tot[0]);
+    double alpha = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->pAp))) : s->rz / s->pAp;
+    s->alpha = alpha;
+    if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
+      s->status = FSIM_ERR_BREAKDOWN;
+      s->done = 1;
+    }
+  }
+}
+
+// Ap = A p_j recomputed from p_j (leaf + face halo); x += alpha p;
+// r -= alpha Ap; r.r and r.z; the last CTA forms beta and the stop test.
+template <typename T, int DM>
+__global__ void __launch_bounds__(kThreads, 12) k_pcg_update(const __grid_constant__ PcgArgs a) {
+  __shared__ T pn[512 + 384];
+  const PcgScalars* sc = a.sc;
+  if (sc->done) return;
+  const int it = sc->iter;
+  const T alpha = T(sc->alpha);
+  const T nalpha = -alpha;
+  const T* p = static_cast<const T*>((it & 1) ? a.p1 : a.p0);
+  T* x = static_cast<T*>(a.x);
+  T* r = static_cast<T*>(a.r);
+  const uint32_t* flags4 = reinterpret_cast<const uint32_t*>(a.flags);
+  const int v0 = threadIdx.x * 4;
+  Dot<DM> drr, drz;
+  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
+    const int32_t* nb = a.nbr + int64_t(s) * 27;
+    const int64_t o = int64_t(s) * 512 + v0;
+    const uint32_t f4 = flags4[o >> 2];
+    const Quad<T> pq = ld4(p, o);
+    const Quad<T> xq = ld4(x, o);
+    const Quad<T> rq = ld4(r, o);
+    T hv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      int q, vox;
+      halo_cell(threadIdx.x + k * kThreads, q, vox);
+      const int ns = nb[q];
+      hv[k] = (ns >= 0 && ns < a.n_pleaf) ? p[int64_t(ns) * 512 + vox] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < 4; ++c) pn[v0 + c] = pq.v[c];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pn[512 + threadIdx.x + k * kThreads] = hv[k];
+    __syncthreads();
+    T ap[4];
+    stencil4(pn, v0, f4, ap);
+    Quad<T> xo, ro;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const uint8_t f = uint8_t(f4 >> (8 * c));
+      xo.v[c] = tadd(tmul(alpha, pq.v[c]), xq.v[c]);
+      ro.v[c] = tadd(tmul(nalpha, ap[c]), rq.v[c]);
+      if (f & 1) {
+        const T z = tmul(inv_diag<T>(f), ro.v[c]);
+        drr.add(ro.v[c], ro.v[c]);
+        drz.add(ro.v[c], z);
+      }
+    }
+    st4(x, o, xo);
+    st4(r, o, ro);
+  }
+  double v[2] = {drr.value(), drz.value()};
+  double tot[2];
+  if (grid_sum<DM, 2>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
+    PcgScalars* s = a.sc;
+    s->rr = round_t(s, tot[0]);
+    s->rz_old = s->rz;
+    s->rz = round_t(s, tot[1]);
+    double beta = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->rz_old))) : s->rz / s->rz_old;
+    s->beta = beta;
+    s->iter = it + 1;
+    if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
+      s->status = FSIM_ERR_BREAKDOWN;
+      s->done = 1;
+    } else {
+      s->done = (s->iter >= s->max_iter) || converged(s, s->rr);
+    }
+  }
+}
+
+// MIXED: x64 += d (inner solution); d is the fp32 x of the inner solve.
+__global__ void k_accumulate_x64(const __grid_constant__ PcgArgs a) {
+  const int64_t n = int64_t(a.n_pleaf) * 512;
+  for (int64_t o = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; o < n;
+       o += int64_t(gridDim.x) * blockDim.x)
+    if (a.flags[o] & 1) a.x64[o] += double(a.dinner[o]);
+}
+
+// MIXED: r64 = b - A x64 in fp64; writes the fp32 rhs of the next inner
+// solve into r and accumulates r64.r64 (fp64) into sc->rr.
+__global__ void __launch_bounds__(kThreads) k_residual64(const __grid_constant__ PcgArgs a) {
+  float* rr32 = static_cast<float*>(a.r);
+  double acc = 0.0;
+  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
+    const int32_t* nb = a.nbr + int64_t(s) * 27;
+    for (int v = threadIdx.x; v < 512; v += kThreads) {
+      const int64_t o = int64_t(s) * 512 + v;
+      const uint8_t f = a.flags[o];
+      if (!(f & 1)) { rr32[o] = 0.f; continue; }
+      const int cx = v >> 6, cy = (v >> 3) & 7, cz = v & 7;
+      double ax = double(flag_diag(f)) * a.x64[o];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        int ux = cx, uy = cy, uz = cz;
+        const int d = (q & 1) ? 1 : -1;
+        if (q < 2) ux += d; else if (q < 4) uy += d; else uz += d;
+        const int sx = ux < 0 ? -1 : (ux > 7 ? 1 : 0), sy = uy < 0 ? -1 : (uy > 7 ? 1 : 0),
+                  sz = uz < 0 ? -1 : (uz > 7 ? 1 : 0);
+        const int ns = nb[(sx + 1) * 9 + (sy + 1) * 3 + (sz + 1)];
+        if (ns < 0 || ns >= a.n_pleaf) continue;
+        const int64_t u = int64_t(ns) * 512 + (((ux & 7) << 6) | ((uy & 7) << 3) | (uz & 7));
+        if (a.flags[u] & 1) ax -= a.x64[u];
+      }
+      const double res = double(a.b[o]) - ax;
+      rr32[o] = float(res);
+      acc += res * res;
+    }
+  }
+  double v[1] = {acc};
+  double tot[1];
+  if (grid_sum<2, 1>(v, a.part, a.maxb, &a.sc->cnt_r, tot) && threadIdx.x == 0) a.sc->rr = tot[0];
+}
+
+template <typename T>
+__global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres, int64_t n) {
+  for (int64_t o = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; o < n;
+       o += int64_t(gridDim.x) * blockDim.x)
+    pres[o] = float(x[o]);
+}
+
+template <typename T, int DM>
+int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const char* nm_spmv,
+              const char* nm_upd) {
+  FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
+  int chunk = 8;
+  for (;;) {
+    FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                               s->stream));
+    FSIM_CK(s, cudaStreamSynchronize(s->stream));
+    if (s->h_sc->done) break;
+    for (int c = 0; c < chunk; ++c) {
+      FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), grid, kThreads, 0, a);
+      FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), grid, kThreads, 0, a);
+    }
+    if (chunk < 64) chunk *= 2;
+  }
+  return FSIM_OK;
+}
+
+int ensure_pcg_vectors(fsim_sim* s, int precision) {
+  const size_t n = size_t(s->cap_pleaf) * 512;
+  if (precision == FSIM_PREC_MIXED && !s->x64) FSIM_CK(s, cudaMalloc(&s->x64, n * sizeof(double)));
+  if (precision == FSIM_PREC_FP64 && !s->r64) {
+    if (!s->x64) FSIM_CK(s, cudaMalloc(&s->x64, n * sizeof(double)));
+    FSIM_CK(s, cudaMalloc(&s->r64, n * sizeof(double)));
+    FSIM_CK(s, cudaMalloc(&s->p64[0], n * sizeof(double)));
+    FSIM_CK(s, cudaMalloc(&s->p64[1], n * sizeof(double)));
+    FSIM_CK(s, cudaMalloc(&s->Ap64, n * sizeof(double)));
+  }
+  return FSIM_OK;
+}
+
+}  // namespace
+
+int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st) {
+  if (!prm) return fail(s, FSIM_ERR_INVALID, "pcg params missing");
+  if (prm->mode < 0 || prm->mode > 2 || prm->precision < 0 || prm->precision > 2)
+    return fail(s, FSIM_ERR_INVALID, "bad pcg mode/precision");
+  int rc = ensure_pcg_vectors(s, prm->precision);
+  if (rc) return rc;
+  const int grid = std::max(1, std::min(s->n_pleaf, s->max_blocks));
+  PcgArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n_pleaf = s->n_pleaf;
+  a.maxb = s->max_blocks;
+  a.nbr = s->d_nbr;
+  a.marker = s->marker;
+  a.b = s->div;
+  a.flags = s->flags;
+  a.sc = s->d_sc;
+  a.part = s->d_part;
+  a.Ap = s->Ap;
+  a.p0 = s->p[0];
+  a.p1 = s->p[1];
+  a.r = s->r;
+  a.x = s->pres;
+  a.x64 = s->x64;
+  a.dinner = s->pres;
+  a.init_r = 1;
+
+  PcgScalars h;
+  memset(&h, 0, sizeof(h));
+  h.mode = prm->mode;
+  h.max_iter = prm->max_iterations;
+  h.fp32 = (prm->precision == FSIM_PREC_FP32);
+  h.thr = prm->threshold;
+  h.tol2 = prm->tolerance * prm->tolerance;
+  int total_it = 0, refinements = 1;
+  int64_t n_rows = 0;
+  double final_rr = 0.0, bb = 0.0;
+  int status = FSIM_OK;
+  const int64_t nvec = int64_t(s->n_pleaf) * 512;
+
+  if (prm->precision == FSIM_PREC_FP32 || prm->precision == FSIM_PREC_FP64) {
+    if (prm->precision == FSIM_PREC_FP64) {
+      a.x = s->x64;
+      a.r = s->r64;
+      a.p0 = s->p64[0];
+      a.p1 = s->p64[1];
+      a.Ap = s->Ap64;
+    }
+    *s->h_sc = h;
+    FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
+                               s->stream));
+    if (prm->precision == FSIM_PREC_FP32)
+      rc = run_inner<float, 0>(s, a, grid, "pcg_setup", "pcg_spmv", "pcg_update");
+    else
+      rc = run_inner<double, 2>(s, a, grid, "pcg_setup_f64", "pcg_spmv_f64", "pcg_update_f64");
+    if (rc) return rc;
+    total_it = s->h_sc->iter;
+    n_rows = int64_t(s->h_sc->n_rows);
+    final_rr = s->h_sc->rr;
+    bb = s->h_sc->bb;
+    status = s->h_sc->status;
+    if (status == FSIM_OK && prm->mode == FSIM_PCG_RELATIVE && !(final_rr <= s->h_sc->thr))
+      status = FSIM_ERR_NOT_CONVERGED;
+    if (prm->precision == FSIM_PREC_FP64)
+      FSIM_LAUNCH(s, "pcg_to_pressure", k_to_pressure<double>,
+                  unsigned(std::min<int64_t>((nvec + 255) / 256, 4096)), 256, 0, s->x64, s->pres,
+                  nvec);
+  } else {
+    // MIXED: fp32 inner Jacobi-PCG with exact dots; fp64 outer refinement.
+    if (nvec > 0) FSIM_CK(s, cudaMemsetAsync(s->x64, 0, size_t(nvec) * sizeof(double), s->stream));
+    // initial residual r = b (x64 = 0): the first inner setup computes flags
+    // and b.b exactly (fp64-accurate), which is the outer b.b.
+    PcgScalars hi = h;
+    hi.mode = FSIM_PCG_RELATIVE;
+    hi.tol2 = prm->inner_tolerance * prm->inner_tolerance;
+    const double tol2 = prm->tolerance * prm->tolerance;
+    refinements = 0;
+    const int max_ref = std::max(1, prm->max_refinements);
+    for (int ref = 0; ref < max_ref; ++ref) {
+      *s->h_sc = hi;
+      FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
+                                 s->stream));
+      a.init_r = (ref == 0) ? 1 : 0;
+      rc = run_inner<float, 1>(s, a, grid, "pcg_setup_mixed", "pcg_spmv_mixed",
+                               "pcg_update_mixed");
+      if (rc) return rc;
+      if (ref == 0) {
+        bb = s->h_sc->bb;
+        n_rows = int64_t(s->h_sc->n_rows);
+      }
+      total_it += s->h_sc->iter;
+      ++refinements;
+      if (s->h_sc->status != FSIM_OK) { status = s->h_sc->status; break; }
+      FSIM_LAUNCH(s, "pcg_accumulate_x64", k_accumulate_x64,
+                  unsigned(std::min<int64_t>((nvec + 255) / 256, 4096)), 256, 0, a);
+      FSIM_LAUNCH(s, "pcg_residual_f64", k_residual64, grid, kThreads, 0, a);
+      FSIM_CK(s, cudaMemcpyAsync(s->h_sc, s->d_sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                 s->stream));
+      FSIM_CK(s, cudaStreamSynchronize(s->stream));
+      final_rr = s->h_sc->rr;
+      if (final_rr <= tol2 * bb) break;
+    }
+    if (status == FSIM_OK && !(final_rr <= tol2 * bb)) status = FSIM_ERR_NOT_CONVERGED;
+    FSIM_LAUNCH(s, "pcg_to_pressure", k_to_pressure<double>,
+                unsigned(std::min<int64_t>((nvec + 255) / 256, 4096)), 256, 0, s->x64, s->pres,
+                nvec);
+  }
+  if (st) {
+    st->iterations = total_it;
+    st->refinements = refinements;
+    st->n_rows = int32_t(n_rows);
+    st->status = status;
+    st->rr = final_rr;
+    st->bb = bb;
+  }
+  return FSIM_OK;
+}
+
+}  // namespace fsim

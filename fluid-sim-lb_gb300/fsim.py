@@ -1,0 +1,418 @@
+"""Python binding of the C ABI in include/fsim.h (ctypes; numpy buffers).
+
+``Simulation`` wraps one fsim_t handle and mirrors the stage methods of the
+reference's ``FlipSimulation`` (schinmayee/fluid-sim-lb,
+common/flip_simulation.h) plus ``PCGDriver::Solve`` (common/solver_driver.h).
+Every call goes through libfsim.so; there is no Python or CPU fallback --
+loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "lib" / "libfsim.so"
+
+OK, ERR_INVALID, ERR_CUDA, ERR_CAPACITY, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_STATE, \
+    ERR_NO_DEVICE, ERR_TIMEOUT = range(9)
+AIR, FLUID, SOLID = 0, 1, 2
+BOUNDARY_BOX, BOUNDARY_TANK = 0, 1
+SHAPE_CUBOID, SHAPE_SPHERE, SHAPE_POOL = 0, 1, 2
+PCG_ABSOLUTE, PCG_RELATIVE, PCG_FIXED = 0, 1, 2
+PREC_FP32, PREC_MIXED, PREC_FP64 = 0, 1, 2
+FIELD_VELOCITY, FIELD_VELOCITY_UPDATE, FIELD_WEIGHT, FIELD_DIVERGENCE, FIELD_PRESSURE, \
+    FIELD_PHI = range(6)
+
+
+class fsim_config(C.Structure):
+    _fields_ = [("global_dims", C.c_int32 * 3), ("boundary", C.c_int32),
+                ("gravity", C.c_float), ("force", C.c_float * 3), ("flip_factor", C.c_float),
+                ("nparticles_per_cell", C.c_int32), ("max_particles", C.c_int64),
+                ("device", C.c_int32)]
+
+
+class fsim_shape(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("a", C.c_float * 3), ("b", C.c_float * 3),
+                ("r", C.c_float)]
+
+
+class fsim_seed_pass(C.Structure):
+    _fields_ = [("nshapes", C.c_int32), ("shapes", fsim_shape * 8), ("velocity", C.c_float * 3)]
+
+
+class fsim_pcg_params(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("precision", C.c_int32), ("max_iterations", C.c_int32),
+                ("max_refinements", C.c_int32), ("threshold", C.c_double),
+                ("tolerance", C.c_double), ("inner_tolerance", C.c_double)]
+
+
+class fsim_pcg_stats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("n_rows", C.c_int32),
+                ("status", C.c_int32), ("rr", C.c_double), ("bb", C.c_double)]
+
+
+class fsim_step_stats(C.Structure):
+    _fields_ = [("particles", C.c_int64), ("particle_leaves", C.c_int32),
+                ("grid_leaves", C.c_int32), ("pcg", fsim_pcg_stats),
+                ("next_inv_speed", C.c_float)]
+
+
+# every symbol include/fsim.h declares, with its ctypes signature
+_P = C.c_void_p
+_SIGS = {
+    "fsim_create": (C.c_int, [C.POINTER(fsim_config), C.POINTER(_P)]),
+    "fsim_destroy": (C.c_int, [_P]),
+    "fsim_last_error": (C.c_char_p, [_P]),
+    "fsim_version": (C.c_char_p, []),
+    "fsim_get_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "fsim_synchronize": (C.c_int, [_P]),
+    "fsim_add_solid_cuboid": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "fsim_seed_fluid": (C.c_int, [_P, C.POINTER(fsim_seed_pass), C.c_int32, C.c_uint64]),
+    "fsim_perturb_velocities": (C.c_int, [_P, C.c_float, C.c_uint64]),
+    "fsim_upload_particles": (C.c_int, [_P, _P, _P, _P, C.c_int64]),
+    "fsim_particle_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "fsim_download_particles": (C.c_int, [_P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "fsim_cfl": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "fsim_move_particles": (C.c_int, [_P, C.c_float]),
+    "fsim_clear_grid": (C.c_int, [_P]),
+    "fsim_transfer_particles_to_grid": (C.c_int, [_P]),
+    "fsim_apply_boundary_conditions": (C.c_int, [_P]),
+    "fsim_save_grid_velocities": (C.c_int, [_P]),
+    "fsim_delete_outside_particles": (C.c_int, [_P]),
+    "fsim_reinitialize_phi": (C.c_int, [_P]),
+    "fsim_add_gravity": (C.c_int, [_P, C.c_float]),
+    "fsim_compute_divergence": (C.c_int, [_P]),
+    "fsim_update_velocity_from_pressure": (C.c_int, [_P]),
+    "fsim_get_velocity_update": (C.c_int, [_P]),
+    "fsim_update_particles_from_grid": (C.c_int, [_P]),
+    "fsim_pcg_default_params": (C.c_int, [_P, C.POINTER(fsim_pcg_params)]),
+    "fsim_pcg_solve": (C.c_int, [_P, C.POINTER(fsim_pcg_params), C.POINTER(fsim_pcg_stats)]),
+    "fsim_step": (C.c_int, [_P, C.c_float, C.POINTER(fsim_pcg_params),
+                            C.POINTER(fsim_step_stats)]),
+    "fsim_compute_dt": (C.c_int, [C.c_float, C.c_int32, C.c_float, C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)]),
+    "fsim_download_field": (C.c_int, [_P, C.c_int32, _P, _P]),
+    "fsim_download_marker": (C.c_int, [_P, _P, _P]),
+    "fsim_download_leaves": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "fsim_set_profiling": (C.c_int, [_P, C.c_int32]),
+    "fsim_get_kernel_times": (C.c_int, [_P, C.POINTER(C.c_char_p), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_int64), C.c_int32,
+                                        C.POINTER(C.c_int32)]),
+    "fsim_reset_kernel_times": (C.c_int, [_P]),
+    "fsim_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+}
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load libfsim.so and bind every declared entry point (raises if absent)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with __graft_entry__.build()")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class FsimError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"fsim error {code}: {msg}")
+        self.code = code
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+@dataclass
+class SceneShape:
+    kind: int
+    a: tuple = (0.0, 0.0, 0.0)
+    b: tuple = (0.0, 0.0, 0.0)
+    r: float = 0.0
+
+
+@dataclass
+class SeedPass:
+    shapes: list
+    velocity: tuple = (0.0, 0.0, 0.0)
+
+    def to_c(self) -> fsim_seed_pass:
+        p = fsim_seed_pass()
+        p.nshapes = len(self.shapes)
+        for i, sh in enumerate(self.shapes):
+            p.shapes[i].kind = sh.kind
+            for d in range(3):
+                p.shapes[i].a[d] = sh.a[d]
+                p.shapes[i].b[d] = sh.b[d]
+            p.shapes[i].r = sh.r
+        for d in range(3):
+            p.velocity[d] = self.velocity[d]
+        return p
+
+
+def pcg_params(mode=PCG_ABSOLUTE, precision=PREC_FP32, max_iterations=1500, threshold=0.0,
+               tolerance=1e-5, inner_tolerance=1e-3, max_refinements=8) -> fsim_pcg_params:
+    p = fsim_pcg_params()
+    p.mode, p.precision, p.max_iterations = mode, precision, max_iterations
+    p.max_refinements = max_refinements
+    p.threshold, p.tolerance, p.inner_tolerance = threshold, tolerance, inner_tolerance
+    return p
+
+
+def compute_dt(inv_speed: float, cfl: int, frame_step: float, time_in_frame: float):
+    """FlipDriver::WhileAndComputeDt rule; returns (dt, new time_in_frame)."""
+    lib = load_library()
+    t = C.c_float(time_in_frame)
+    dt = C.c_float(0.0)
+    rc = lib.fsim_compute_dt(C.c_float(inv_speed), cfl, C.c_float(frame_step), C.byref(t),
+                             C.byref(dt))
+    if rc:
+        raise FsimError(rc, "compute_dt")
+    return dt.value, t.value
+
+
+class Simulation:
+    """One simulation domain on one GPU (a fsim_t handle)."""
+
+    def __init__(self, dims, boundary=BOUNDARY_BOX, gravity=9.8, force=(0.0, 9.8, 0.0),
+                 flip=0.95, nppc=8, max_particles=0, device=0):
+        self.lib = load_library()
+        cfg = fsim_config()
+        for d in range(3):
+            cfg.global_dims[d] = int(dims[d])
+            cfg.force[d] = float(force[d])
+        cfg.boundary = boundary
+        cfg.gravity = gravity
+        cfg.flip_factor = flip
+        cfg.nparticles_per_cell = nppc
+        cfg.max_particles = max_particles
+        cfg.device = device
+        self.dims = tuple(int(x) for x in dims)
+        h = C.c_void_p()
+        rc = self.lib.fsim_create(C.byref(cfg), C.byref(h))
+        if rc:
+            raise FsimError(rc, "fsim_create failed")
+        self.h = h
+
+    # -- plumbing ---------------------------------------------------------
+    def _ck(self, rc: int, what: str = ""):
+        if rc:
+            raise FsimError(rc, f"{what}: {self.lib.fsim_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fsim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def synchronize(self):
+        self._ck(self.lib.fsim_synchronize(self.h), "synchronize")
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._ck(self.lib.fsim_get_stream(self.h, C.byref(s)), "get_stream")
+        return s.value or 0
+
+    # -- scene ------------------------------------------------------------
+    def add_solid_cuboid(self, lo, hi):
+        a = (C.c_int32 * 3)(*lo)
+        b = (C.c_int32 * 3)(*hi)
+        self._ck(self.lib.fsim_add_solid_cuboid(self.h, a, b), "add_solid_cuboid")
+
+    def seed(self, passes: list[SeedPass], seed: int = 0):
+        arr = (fsim_seed_pass * max(1, len(passes)))()
+        for i, p in enumerate(passes):
+            arr[i] = p.to_c()
+        self._ck(self.lib.fsim_seed_fluid(self.h, arr, len(passes), C.c_uint64(seed)), "seed")
+
+    def perturb_velocities(self, sigma: float, seed: int):
+        self._ck(self.lib.fsim_perturb_velocities(self.h, C.c_float(sigma), C.c_uint64(seed)),
+                 "perturb")
+
+    def upload_particles(self, pos, vel, gvel):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        gvel = np.ascontiguousarray(gvel, dtype=np.float32)
+        n = pos.shape[0]
+        self._ck(self.lib.fsim_upload_particles(self.h, _ptr(pos), _ptr(vel), _ptr(gvel), n),
+                 "upload")
+
+    def particle_count(self) -> int:
+        n = C.c_int64()
+        self._ck(self.lib.fsim_particle_count(self.h, C.byref(n)), "particle_count")
+        return n.value
+
+    def download_particles(self):
+        n = self.particle_count()
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        gvel = np.empty((n, 3), np.float32)
+        got = C.c_int64()
+        self._ck(self.lib.fsim_download_particles(self.h, _ptr(pos), _ptr(vel), _ptr(gvel), n,
+                                                  C.byref(got)), "download_particles")
+        return pos, vel, gvel
+
+    # -- stages (FlipSimulation methods) ------------------------------------
+    def cfl(self) -> float:
+        v = C.c_float()
+        self._ck(self.lib.fsim_cfl(self.h, C.byref(v)), "cfl")
+        return v.value
+
+    def move_particles(self, dt):
+        self._ck(self.lib.fsim_move_particles(self.h, C.c_float(dt)), "move_particles")
+
+    def clear_grid(self):
+        self._ck(self.lib.fsim_clear_grid(self.h), "clear_grid")
+
+    def transfer_particles_to_grid(self):
+        self._ck(self.lib.fsim_transfer_particles_to_grid(self.h), "p2g")
+
+    def apply_boundary_conditions(self):
+        self._ck(self.lib.fsim_apply_boundary_conditions(self.h), "bc")
+
+    def save_grid_velocities(self):
+        self._ck(self.lib.fsim_save_grid_velocities(self.h), "save")
+
+    def delete_outside_particles(self):
+        self._ck(self.lib.fsim_delete_outside_particles(self.h), "delete_outside")
+
+    def reinitialize_phi(self):
+        self._ck(self.lib.fsim_reinitialize_phi(self.h), "reinit_phi")
+
+    def add_gravity(self, dt):
+        self._ck(self.lib.fsim_add_gravity(self.h, C.c_float(dt)), "gravity")
+
+    def compute_divergence(self):
+        self._ck(self.lib.fsim_compute_divergence(self.h), "divergence")
+
+    def update_velocity_from_pressure(self):
+        self._ck(self.lib.fsim_update_velocity_from_pressure(self.h), "pressure_update")
+
+    def get_velocity_update(self):
+        self._ck(self.lib.fsim_get_velocity_update(self.h), "velocity_update")
+
+    def update_particles_from_grid(self):
+        self._ck(self.lib.fsim_update_particles_from_grid(self.h), "g2p")
+
+    def default_pcg_params(self) -> fsim_pcg_params:
+        p = fsim_pcg_params()
+        self._ck(self.lib.fsim_pcg_default_params(self.h, C.byref(p)), "pcg_default")
+        return p
+
+    def pcg_solve(self, params: fsim_pcg_params) -> fsim_pcg_stats:
+        st = fsim_pcg_stats()
+        self._ck(self.lib.fsim_pcg_solve(self.h, C.byref(params), C.byref(st)), "pcg_solve")
+        return st
+
+    def step(self, dt: float, params: fsim_pcg_params) -> fsim_step_stats:
+        st = fsim_step_stats()
+        self._ck(self.lib.fsim_step(self.h, C.c_float(dt), C.byref(params), C.byref(st)), "step")
+        return st
+
+    # -- downloads ----------------------------------------------------------
+    def _dense_shape(self):
+        return tuple(d + 2 for d in self.dims)
+
+    def field(self, which: int):
+        shp = self._dense_shape()
+        vec = which in (FIELD_VELOCITY, FIELD_VELOCITY_UPDATE, FIELD_WEIGHT)
+        out = np.empty(shp + ((3,) if vec else ()), np.float32)
+        act = np.empty(shp, np.uint8)
+        self._ck(self.lib.fsim_download_field(self.h, which, _ptr(out), _ptr(act)), "field")
+        return out, act
+
+    def marker(self):
+        shp = self._dense_shape()
+        out = np.empty(shp, np.int32)
+        act = np.empty(shp, np.uint8)
+        self._ck(self.lib.fsim_download_marker(self.h, _ptr(out), _ptr(act)), "marker")
+        return out, act
+
+    def leaves(self):
+        n = C.c_int64()
+        cap = max(1, self.particle_count())
+        out = np.empty((cap, 3), np.int32)
+        self._ck(self.lib.fsim_download_leaves(self.h, _ptr(out), cap, C.byref(n)), "leaves")
+        return out[: n.value].copy()
+
+    # -- timing -------------------------------------------------------------
+    def set_profiling(self, on: bool):
+        self._ck(self.lib.fsim_set_profiling(self.h, 1 if on else 0), "profiling")
+
+    def kernel_times(self) -> dict:
+        cnt = C.c_int32()
+        self._ck(self.lib.fsim_get_kernel_times(self.h, None, None, None, 0, C.byref(cnt)), "kt")
+        n = cnt.value
+        names = (C.c_char_p * max(1, n))()
+        ms = (C.c_double * max(1, n))()
+        la = (C.c_int64 * max(1, n))()
+        self._ck(self.lib.fsim_get_kernel_times(self.h, names, ms, la, n, C.byref(cnt)), "kt")
+        return {names[i].decode(): (ms[i], la[i]) for i in range(n)}
+
+    def reset_kernel_times(self):
+        self._ck(self.lib.fsim_reset_kernel_times(self.h), "reset_kt")
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._ck(self.lib.fsim_launch_count(self.h, C.byref(n)), "launch_count")
+        return n.value
+
+
+# ---- synthetic scenes of the benchmark configurations ----------------------
+def scene_passes(name: str, n: int) -> list[SeedPass]:
+    """Seeding passes (index space) for the named synthetic scene at N^3.
+
+    sphere_drop: sphere r=0.15 at (0.5,0.7,0.5) over a pool y<0.2
+    dam_break:   block x<0.4, y<0.6, all z
+    multidam:    four 0.2x0.5x0.2 blocks at the x/z quadrant corners + pool y<0.05
+    sphere_pool: sphere r=0.1 at (0.5,0.6,0.5) + pool y<0.1
+    """
+    N = float(n)
+    if name == "sphere_drop":
+        return [SeedPass([SceneShape(SHAPE_POOL, a=(0.0, 0.2 * N, 0.0)),
+                          SceneShape(SHAPE_SPHERE, a=(0.5 * N, 0.7 * N, 0.5 * N), r=0.15 * N)])]
+    if name == "dam_break":
+        return [SeedPass([SceneShape(SHAPE_CUBOID, a=(0.0, 0.0, 0.0), b=(0.4 * N, 0.6 * N, N))])]
+    if name == "multidam":
+        shapes = [SceneShape(SHAPE_POOL, a=(0.0, 0.05 * N, 0.0))]
+        for x0 in (0.0, 0.8):
+            for z0 in (0.0, 0.8):
+                shapes.append(SceneShape(SHAPE_CUBOID, a=(x0 * N, 0.0, z0 * N),
+                                         b=((x0 + 0.2) * N, 0.5 * N, (z0 + 0.2) * N)))
+        return [SeedPass(shapes)]
+    if name == "sphere_pool":
+        return [SeedPass([SceneShape(SHAPE_POOL, a=(0.0, 0.1 * N, 0.0)),
+                          SceneShape(SHAPE_SPHERE, a=(0.5 * N, 0.6 * N, 0.5 * N), r=0.1 * N)])]
+    raise ValueError(name)
+
+
+def physical_gravity(n: int) -> tuple[float, tuple]:
+    """Gravity -9.8 with dx = 1/N in index space: 9.8*N cells/s^2."""
+    g = float(np.float32(9.8 * n))
+    return g, (0.0, g, 0.0)

@@ -1,0 +1,259 @@
+/*
+ * fsim.h -- C ABI of the GB300-native FLIP step hot path.
+ *
+ * One handle (fsim_t) owns the device state of one simulation domain: the
+ * particle store (SoA, sorted by cell in OpenVDB leaf iteration order), the
+ * sparse 8^3 brick layout (active-leaf list, 27-entry neighbour table, per-leaf
+ * per-cell particle ranges) and the grid fields stored per leaf.  A handle is
+ * bound to one CUDA stream and is not thread-safe.  Every entry point returns
+ * an int status (FSIM_OK on success); fsim_last_error() gives the message.
+ * Host buffers passed in are copied; the handle owns all device memory.
+ *
+ * Index space: voxel length 1, cell (i,j,k) covers [i,i+1)x[j,j+1)x[k,k+1),
+ * the domain is [0,N) per axis, solid walls are the cells at -1 and N.  MAC
+ * staggering: vel(i,j,k)[0] is the x-face at x=i centred at (j+.5,k+.5), and
+ * likewise for y and z.  Dense downloads cover voxels [-1,N] per axis and use
+ * the linear index ((i+1)*(N1+2) + (j+1))*(N2+2) + (k+1).
+ *
+ * Each stage function names the reference member function it replaces
+ * (schinmayee/fluid-sim-lb, paths relative to that project).
+ */
+#ifndef FSIM_H
+#define FSIM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  FSIM_OK = 0,
+  FSIM_ERR_INVALID = 1,        /* bad argument or configuration */
+  FSIM_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+  FSIM_ERR_CAPACITY = 3,       /* particle / leaf capacity exceeded */
+  FSIM_ERR_NOT_CONVERGED = 4,  /* PCG hit max iterations (relative mode) */
+  FSIM_ERR_BREAKDOWN = 5,      /* PCG alpha or beta > 1e5 or not finite
+                                  (replaces CHECK_LE(alpha, LARGE_FLOAT),
+                                  common/solver.cc:333,361) */
+  FSIM_ERR_STATE = 6,          /* call order violated */
+  FSIM_ERR_NO_DEVICE = 7,      /* no CUDA device visible */
+  FSIM_ERR_TIMEOUT = 8         /* a bounded device-side wait ran out */
+};
+
+/* CellType, common/definitions.h:6 */
+enum { FSIM_AIR = 0, FSIM_FLUID = 1, FSIM_SOLID = 2 };
+
+/* Boundary kind, FlipApp config "boundary", common/flip_app_sim.cc:105-112 */
+enum { FSIM_BOUNDARY_BOX = 0, FSIM_BOUNDARY_TANK = 1 };
+
+typedef struct fsim_sim fsim_t;
+
+/* Simulation parameters.  Mirrors FlipSimulation::InitializeMetadata
+ * (common/flip_simulation.cc:84-101) and SetForces (:249-253).  gravity and
+ * force are index-space values the caller has already scaled (the reference
+ * scales by N/128, common/flip_app_sim.cc:74,87). */
+typedef struct fsim_config {
+  int32_t global_dims[3];      /* cells per axis, 8 <= N <= 1024 */
+  int32_t boundary;            /* FSIM_BOUNDARY_* */
+  float gravity;               /* gravity_ used by CFL(): sqrt(0.5*gravity) */
+  float force[3];              /* fx_,fy_,fz_: AddGravity adds dt*(fx,-fy,fz) */
+  float flip_factor;           /* FLIP/PIC blend */
+  int32_t nparticles_per_cell; /* seeding target */
+  int64_t max_particles;       /* particle capacity (0: 9 per domain cell,
+                                  capped to fit) */
+  int32_t device;              /* CUDA device ordinal */
+} fsim_config;
+
+int fsim_create(const fsim_config* cfg, fsim_t** out);
+int fsim_destroy(fsim_t* sim);
+const char* fsim_last_error(const fsim_t* sim); /* sim may be NULL */
+/* Library version string, never NULL. */
+const char* fsim_version(void);
+
+/* Raw cudaStream_t the handle launches on. */
+int fsim_get_stream(fsim_t* sim, void** stream);
+int fsim_synchronize(fsim_t* sim);
+
+/* ---- solids (static) --------------------------------------------------- */
+/* FlipSimulation::AddSolidCuboid, common/flip_simulation.cc:316-324: the
+ * inclusive integer box [lo,hi] intersected with the domain grown by one
+ * cell.  Box/tank walls come from cfg->boundary (SetBoxBoundary :256-308,
+ * SetTankBoundary :332-377).  At most 32 cuboids. */
+int fsim_add_solid_cuboid(fsim_t* sim, const int32_t lo[3], const int32_t hi[3]);
+
+/* ---- scene seeding (setup, not part of a step) ------------------------- */
+/* A seeding pass restates FlipSimulation::InitializePhiAndParticles
+ * (common/flip_simulation.cc:139-188) for phi = min over the pass's shapes:
+ * each non-solid cell whose centre has phi < 0 gets up to
+ * nparticles_per_cell particles drawn uniformly in the cell (at most 32
+ * draws, a draw is kept where phi(p) <= 0), unless the cell already holds
+ * that many.  glibc random() is replaced by a counter-based SplitMix64
+ * stream keyed by (seed, pass, cell, draw).  Shapes (index space):
+ *   CUBOID: a = start, b = end, phi = inside(inclusive) ? -1 : 1 (:222-233)
+ *   SPHERE: a = centre, r = radius, phi = |p-a| - r                (:236-246)
+ *   POOL:   a[1] = height, phi = p.y - height                       (:200-219) */
+enum { FSIM_SHAPE_CUBOID = 0, FSIM_SHAPE_SPHERE = 1, FSIM_SHAPE_POOL = 2 };
+typedef struct fsim_shape {
+  int32_t kind;
+  float a[3];
+  float b[3];
+  float r;
+} fsim_shape;
+#define FSIM_MAX_SHAPES 8
+typedef struct fsim_seed_pass {
+  int32_t nshapes;
+  fsim_shape shapes[FSIM_MAX_SHAPES];
+  float velocity[3];           /* initial velocity and grid_velocity */
+} fsim_seed_pass;
+int fsim_seed_fluid(fsim_t* sim, const fsim_seed_pass* passes, int32_t npasses,
+                    uint64_t seed);
+/* Adds N(0, sigma^2) per component to particle velocity and grid_velocity
+ * (same draw for both), counter-based stream keyed by (seed, particle rank). */
+int fsim_perturb_velocities(fsim_t* sim, float sigma, uint64_t seed);
+
+/* ---- particle I/O ------------------------------------------------------ */
+/* pos/vel/gvel are n xyz triples (AoS float[3*n]).  Upload rebins (stable
+ * sort by cell in OpenVDB leaf order) and rebuilds the brick topology. */
+int fsim_upload_particles(fsim_t* sim, const float* pos, const float* vel,
+                          const float* gvel, int64_t n);
+int fsim_particle_count(fsim_t* sim, int64_t* n);
+/* Live particles in cell order (the reference's iteration order).
+ * Any of pos/vel/gvel may be NULL.  Fails with FSIM_ERR_CAPACITY when the
+ * count exceeds capacity (n is still written). */
+int fsim_download_particles(fsim_t* sim, float* pos, float* vel, float* gvel,
+                            int64_t capacity, int64_t* n);
+
+/* ---- per-stage entry points (FlipSimulation member functions) ---------- */
+/* FlipSimulation::CFL, common/flip_simulation.cc:460-488: returns 1/v with
+ * v = max(sqrt(0.5*gravity), max |v_d| over active in-box faces), v>=1e-2. */
+int fsim_cfl(fsim_t* sim, float* inv_speed);
+/* Particles::StepInGrid<VectorGrid,true,1,1> (common/particles.cc:479-546)
+ * followed by Particles::DeleteParticlesInSolids (:202-219). */
+int fsim_move_particles(fsim_t* sim, float dt);
+/* FlipSimulation::ClearGridData, common/flip_simulation.cc:380-389 */
+int fsim_clear_grid(fsim_t* sim);
+/* FlipSimulation::TransferParticlesToGrid, :809-923 (marker FLUID, weighted
+ * velocity, weight, normalisation with the 1e-5 cut). */
+int fsim_transfer_particles_to_grid(fsim_t* sim);
+/* FlipSimulation::ApplyBoundaryConditions, :657-713 */
+int fsim_apply_boundary_conditions(fsim_t* sim);
+/* FlipSimulation::SaveGridVelocities, :491-496 */
+int fsim_save_grid_velocities(fsim_t* sim);
+/* Particles::DeleteOutsideParticles, common/particles.cc:273-293 */
+int fsim_delete_outside_particles(fsim_t* sim);
+/* FlipSimulation::ReinitializePhiSimple, :529-539 */
+int fsim_reinitialize_phi(fsim_t* sim);
+/* FlipSimulation::AddGravity, :506-515 */
+int fsim_add_gravity(fsim_t* sim, float dt);
+/* FlipSimulation::ComputeDivergence, :716-736 */
+int fsim_compute_divergence(fsim_t* sim);
+/* FlipSimulation::UpdateVelocityFromPressure, :739-778 */
+int fsim_update_velocity_from_pressure(fsim_t* sim);
+/* FlipSimulation::GetVelocityUpdate, :781-801 */
+int fsim_get_velocity_update(fsim_t* sim);
+/* FlipSimulation::UpdateParticlesFromGrid, :1025-1091, including both
+ * VectorGrid::ExtrapolateToBoundary calls (common/vector_grid.cc:302-381). */
+int fsim_update_particles_from_grid(fsim_t* sim);
+
+/* ---- pressure solve (PCGDriver::Solve, common/solver_driver.cc:14-69) --- */
+enum {
+  FSIM_PCG_ABSOLUTE = 0, /* reference rule: stop when r.r < threshold or
+                            iterations >= max (solver_driver.cc:319-337) */
+  FSIM_PCG_RELATIVE = 1, /* stop when ||r||/||b|| <= tolerance */
+  FSIM_PCG_FIXED = 2     /* exactly max_iterations (fixed_iterations_) */
+};
+enum {
+  FSIM_PREC_FP32 = 0,  /* reference: fp32 vectors and fp32 dot products */
+  FSIM_PREC_MIXED = 1, /* fp32 inner PCG with FP64-accumulated dots and an
+                          FP64 outer residual refinement r = b - A x */
+  FSIM_PREC_FP64 = 2   /* fp64 vectors and dots */
+};
+typedef struct fsim_pcg_params {
+  int32_t mode;            /* FSIM_PCG_* */
+  int32_t precision;       /* FSIM_PREC_* */
+  int32_t max_iterations;  /* per inner solve (reference default 1500) */
+  int32_t max_refinements; /* MIXED: outer refinement sweeps (>=1) */
+  double threshold;        /* ABSOLUTE: r.r threshold (reference N^3*0.5e-8) */
+  double tolerance;        /* RELATIVE: ||r||/||b|| target (outer, MIXED) */
+  double inner_tolerance;  /* MIXED: relative target of each inner solve */
+} fsim_pcg_params;
+typedef struct fsim_pcg_stats {
+  int32_t iterations;      /* total inner iterations */
+  int32_t refinements;     /* outer sweeps (MIXED), else 1 */
+  int32_t n_rows;          /* fluid cells (PCG unknowns) */
+  int32_t status;          /* FSIM_OK / NOT_CONVERGED / BREAKDOWN */
+  double rr;               /* final r.r (fp64 residual in MIXED) */
+  double bb;               /* b.b */
+} fsim_pcg_stats;
+/* Fills params with the reference defaults for the handle's domain:
+ * ABSOLUTE, FP32, 1500 iterations, threshold N1*N2*N3*0.5e-8
+ * (common/flip_app.cc:325-332, common/flip_app.h:52-53). */
+int fsim_pcg_default_params(const fsim_t* sim, fsim_pcg_params* params);
+/* Builds A from the marker (7-point Laplacian, SOLID neighbours excluded,
+ * common/solver.cc:198-233), b from the divergence, x0 = 0, runs Jacobi PCG
+ * and writes the pressure grid (CopySolution, solver.cc:94-99). */
+int fsim_pcg_solve(fsim_t* sim, const fsim_pcg_params* params,
+                   fsim_pcg_stats* stats);
+
+/* ---- one step (FlipDriver::RunOneStep, common/flip_app_sim.cc:211-254) -- */
+typedef struct fsim_step_stats {
+  int64_t particles;       /* live particles after the step */
+  int32_t particle_leaves; /* 8^3 leaves holding particles */
+  int32_t grid_leaves;     /* leaves holding grid values (dilated by 1) */
+  fsim_pcg_stats pcg;
+  float next_inv_speed;    /* CFL() of the velocity left by this step */
+} fsim_step_stats;
+/* MoveParticles(dt) + DeleteParticlesInSolids, ClearGridData,
+ * TransferParticlesToGrid, ApplyBoundaryConditions, SaveGridVelocities,
+ * DeleteOutsideParticles, ReinitializePhiSimple, AddGravity(dt),
+ * ApplyBoundaryConditions, ComputeDivergence, PCG solve,
+ * UpdateVelocityFromPressure, GetVelocityUpdate, UpdateParticlesFromGrid --
+ * run as fused device kernels.  stats may be NULL. */
+int fsim_step(fsim_t* sim, float dt, const fsim_pcg_params* params,
+              fsim_step_stats* stats);
+
+/* Global dt rule of FlipDriver::WhileAndComputeDt (flip_app_sim.cc:357-428)
+ * for one partition: dt = min(cfl*inv_speed, 1/frame_step), raised to
+ * frame_step/10, clipped to the frame end (also when it would pass 0.9 of
+ * the frame).  *time_in_frame is advanced by dt.  Host-only. */
+int fsim_compute_dt(float inv_speed, int32_t cfl, float frame_step,
+                    float* time_in_frame, float* dt);
+
+/* ---- dense downloads (parity / output) -------------------------------- */
+enum {
+  FSIM_FIELD_VELOCITY = 0,        /* grid_velocity_ (Vec3) */
+  FSIM_FIELD_VELOCITY_UPDATE = 1, /* grid_velocity_update_ (Vec3) */
+  FSIM_FIELD_WEIGHT = 2,          /* grid_weight_ (Vec3) */
+  FSIM_FIELD_DIVERGENCE = 3,      /* grid_divergence_ (scalar) */
+  FSIM_FIELD_PRESSURE = 4,        /* grid_pressure_ (scalar) */
+  FSIM_FIELD_PHI = 5              /* grid_phi_ (scalar, background 5) */
+};
+/* Vec3 fields: out has 3*(N1+2)(N2+2)(N3+2) floats (xyz per voxel); scalar
+ * fields one float per voxel.  active (nullable) gets 1 byte per voxel:
+ * the OpenVDB active state.  Inactive voxels read the background. */
+int fsim_download_field(fsim_t* sim, int32_t field, float* out, uint8_t* active);
+/* grid_marker_ as int32 per voxel (AIR background), active per voxel. */
+int fsim_download_marker(fsim_t* sim, int32_t* out, uint8_t* active);
+/* Particle-tree leaf topology: origins (xyz triples, cells) of the 8^3
+ * leaves holding particles, in OpenVDB leaf iteration order. */
+int fsim_download_leaves(fsim_t* sim, int32_t* origins, int64_t capacity,
+                         int64_t* n);
+
+/* ---- kernel timing (CUDA events on the handle's stream) --------------- */
+int fsim_set_profiling(fsim_t* sim, int32_t enabled);
+/* Accumulated per-kernel device time since the last reset.  Writes up to
+ * capacity entries; names are static strings owned by the library. */
+int fsim_get_kernel_times(fsim_t* sim, const char** names, double* total_ms,
+                          int64_t* launches, int32_t capacity, int32_t* count);
+int fsim_reset_kernel_times(fsim_t* sim);
+/* Number of library kernel launches issued on this handle so far. */
+int fsim_launch_count(fsim_t* sim, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FSIM_H */

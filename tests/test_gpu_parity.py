@@ -1,0 +1,242 @@
+"""GPU parity: every stage of the FLIP step through the C ABI vs the oracle.
+
+Bars: particle binning, leaf topology, activation masks and markers are
+bit-exact; advected positions are bit-exact (same input state); velocities
+and pressures agree within 1e-5 relative L2 (FIELD_RTOL).
+"""
+import numpy as np
+import pytest
+
+import fsim
+from _util import FIELD_RTOL, assert_marker, assert_vec_field, make_gpu, make_oracle, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+SCENES = [
+    dict(n=20, scene="sphere_drop", boundary=fsim.BOUNDARY_BOX, solids=()),
+    dict(n=32, scene="dam_break", boundary=fsim.BOUNDARY_BOX, solids=(((12, 0, 12), (17, 5, 19)),)),
+    dict(n=24, scene="sphere_drop", boundary=fsim.BOUNDARY_TANK, solids=()),
+]
+
+
+def _noise(n):
+    return 0.3 * n
+
+
+@pytest.mark.parametrize("n,scene", [(20, "sphere_drop"), (40, "multidam"), (33, "dam_break")])
+def test_seed_bitexact(n, scene):
+    orc = make_oracle(n, scene)
+    g, f = fsim.physical_gravity(n)
+    with fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f) as sim:
+        sim.seed(fsim.scene_passes(scene, n), seed=0)
+        p1, v1, g1 = sim.download_particles()
+    p0, v0, g0 = orc.particles()
+    assert p1.shape == p0.shape
+    assert np.array_equal(p1, p0)
+    assert np.array_equal(v1, v0) and np.array_equal(g1, g0)
+
+
+def test_seed_skips_solid_cells_and_counts_passes():
+    n = 16
+    g, f = fsim.physical_gravity(n)
+    solids = (((4, 0, 4), (9, 3, 9)),)
+    orc = make_oracle(n, "dam_break", solids=solids)
+    passes = fsim.scene_passes("dam_break", n) + fsim.scene_passes("sphere_drop", n)
+    orc.seed(passes, seed=5)
+    with fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f) as sim:
+        for lo, hi in solids:
+            sim.add_solid_cuboid(lo, hi)
+        sim.seed(passes, seed=5)
+        p1, _, _ = sim.download_particles()
+    p0, _, _ = orc.particles()
+    assert np.array_equal(p1, p0)
+
+
+@pytest.mark.parametrize("cfg", SCENES, ids=lambda c: f"{c['scene']}{c['n']}b{c['boundary']}")
+def test_upload_topology_bitexact(cfg):
+    orc = make_oracle(cfg["n"], cfg["scene"], cfg["boundary"], cfg["solids"], noise=1.0)
+    sim = make_gpu(orc, cfg["boundary"], cfg["solids"])
+    p1, v1, g1 = sim.download_particles()
+    p0, v0, g0 = orc.particles()
+    assert np.array_equal(p1, p0) and np.array_equal(v1, v0) and np.array_equal(g1, g0)
+    assert np.array_equal(sim.leaves(), orc.leaves())
+    sim.close()
+
+
+@pytest.mark.parametrize("cfg", SCENES, ids=lambda c: f"{c['scene']}{c['n']}b{c['boundary']}")
+def test_move_particles_bitexact(cfg):
+    n = cfg["n"]
+    orc = make_oracle(n, cfg["scene"], cfg["boundary"], cfg["solids"], noise=3.0 * n)
+    sim = make_gpu(orc, cfg["boundary"], cfg["solids"])
+    for dt in (0.01, 0.05):
+        sim.move_particles(dt)
+        orc.move_particles(dt)
+        p1, v1, g1 = sim.download_particles()
+        p0, v0, g0 = orc.particles()
+        assert p1.shape == p0.shape, "particle deletion in solids differs"
+        assert np.array_equal(p1, p0), "advected/clamped positions differ"
+        assert np.array_equal(v1, v0)
+        assert np.array_equal(sim.leaves(), orc.leaves()), "leaf topology differs"
+    sim.close()
+
+
+def _stagewise(cfg, dt=0.01):
+    n = cfg["n"]
+    orc = make_oracle(n, cfg["scene"], cfg["boundary"], cfg["solids"], noise=_noise(n))
+    sim = make_gpu(orc, cfg["boundary"], cfg["solids"])
+    return orc, sim
+
+
+@pytest.mark.parametrize("cfg", SCENES, ids=lambda c: f"{c['scene']}{c['n']}b{c['boundary']}")
+def test_stagewise_parity(cfg):
+    orc, sim = _stagewise(cfg)
+    dt = 0.01
+    for o in (orc, sim):
+        o.move_particles(dt)
+        o.clear_grid()
+        o.transfer_particles_to_grid()
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY, 1e-6, label="p2g velocity")
+    assert_vec_field(sim, orc, fsim.FIELD_WEIGHT, 1e-6, label="p2g weight")
+    assert_marker(sim, orc, "p2g marker")
+    for o in (orc, sim):
+        o.apply_boundary_conditions()
+        o.save_grid_velocities()
+        o.delete_outside_particles()
+        o.reinitialize_phi()
+        o.add_gravity(dt)
+        o.apply_boundary_conditions()
+    assert_marker(sim, orc, "bc marker")
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY, 1e-6, label="bc+gravity velocity")
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY_UPDATE, 1e-6, label="saved velocity")
+    a, aa = sim.field(fsim.FIELD_PHI)
+    b, ba = orc.field(5)
+    assert np.array_equal(aa, ba) and np.array_equal(a, b)
+    for o in (orc, sim):
+        o.compute_divergence()
+    a, aa = sim.field(fsim.FIELD_DIVERGENCE)
+    b, ba = orc.field(3)
+    assert np.array_equal(aa, ba)
+    assert rel_l2(a, b) <= 1e-6
+    # converged solves on both sides (fp64 oracle vs mixed GPU)
+    st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 2000,
+                                       tolerance=1e-10, inner_tolerance=1e-4))
+    ost = orc.pcg_solve(mode=1, precision=2, max_iterations=20000, tol=1e-13)
+    assert st.status == 0 and ost.status == 0
+    a, aa = sim.field(fsim.FIELD_PRESSURE)
+    b, ba = orc.field(4)
+    assert np.array_equal(aa, ba)
+    assert rel_l2(a, b) <= 1e-6
+    for o in (orc, sim):
+        o.update_velocity_from_pressure()
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY, FIELD_RTOL, label="projected velocity")
+    sim.get_velocity_update()
+    assert orc.get_velocity_update() == 0
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY_UPDATE, FIELD_RTOL, label="velocity update")
+    for o in (orc, sim):
+        o.update_particles_from_grid()
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY, FIELD_RTOL, label="extrapolated velocity")
+    assert_vec_field(sim, orc, fsim.FIELD_VELOCITY_UPDATE, FIELD_RTOL, label="extrapolated dv")
+    p1, v1, g1 = sim.download_particles()
+    p0, v0, g0 = orc.particles()
+    assert np.array_equal(p1, p0)
+    assert rel_l2(v1, v0) <= FIELD_RTOL
+    assert rel_l2(g1, g0) <= FIELD_RTOL
+    sim.close()
+
+
+def test_cfl_matches():
+    orc, sim = _stagewise(SCENES[1])
+    assert sim.cfl() == orc.cfl()  # empty grid: sqrt(0.5 g) rule
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 2000, tolerance=1e-10,
+                          inner_tolerance=1e-4)
+    sim.step(0.01, prm)
+    orc.step(0.01, mode=1, precision=2, max_iterations=20000, tol=1e-13)
+    a, b = sim.cfl(), orc.cfl()
+    assert abs(a - b) <= 1e-5 * abs(b)
+    sim.close()
+
+
+@pytest.mark.parametrize("cfg", SCENES, ids=lambda c: f"{c['scene']}{c['n']}b{c['boundary']}")
+def test_fused_step_replay(cfg):
+    """Per-step replay: same state into fsim_step and the oracle's RunOneStep."""
+    orc, sim = _stagewise(cfg)
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 2000, tolerance=1e-10,
+                          inner_tolerance=1e-4)
+    for k in range(3):
+        dt = 0.004 + 0.003 * k
+        st = sim.step(dt, prm)
+        orc.step(dt, mode=1, precision=2, max_iterations=20000, tol=1e-13)
+        p1, v1, g1 = sim.download_particles()
+        p0, v0, g0 = orc.particles()
+        assert p1.shape == p0.shape and st.particles == p0.shape[0]
+        assert np.array_equal(p1, p0)
+        assert rel_l2(v1, v0) <= FIELD_RTOL
+        assert rel_l2(g1, g0) <= FIELD_RTOL
+        assert_marker(sim, orc, f"step {k} marker")
+        assert_vec_field(sim, orc, fsim.FIELD_VELOCITY, FIELD_RTOL, label=f"step {k} velocity")
+        assert_vec_field(sim, orc, fsim.FIELD_VELOCITY_UPDATE, FIELD_RTOL, label=f"step {k} dv")
+        a, _ = sim.field(fsim.FIELD_PRESSURE)
+        b, _ = orc.field(4)
+        assert rel_l2(a, b) <= FIELD_RTOL
+        # replay: feed the oracle's state to both for the next step
+        sim.upload_particles(p0, v0, g0)
+    sim.close()
+
+
+def test_fused_equals_staged_gpu():
+    cfg = SCENES[0]
+    orc = make_oracle(cfg["n"], cfg["scene"], noise=_noise(cfg["n"]))
+    a = make_gpu(orc)
+    b = make_gpu(orc)
+    prm = fsim.pcg_params(fsim.PCG_FIXED, fsim.PREC_FP32, 40)
+    dt = 0.01
+    a.step(dt, prm)
+    b.move_particles(dt)
+    b.clear_grid()
+    b.transfer_particles_to_grid()
+    b.apply_boundary_conditions()
+    b.save_grid_velocities()
+    b.delete_outside_particles()
+    b.reinitialize_phi()
+    b.add_gravity(dt)
+    b.apply_boundary_conditions()
+    b.compute_divergence()
+    b.pcg_solve(prm)
+    b.update_velocity_from_pressure()
+    b.get_velocity_update()
+    b.update_particles_from_grid()
+    pa, va, ga = a.download_particles()
+    pb, vb, gb = b.download_particles()
+    assert np.array_equal(pa, pb)
+    assert rel_l2(va, vb) <= 1e-6 and rel_l2(ga, gb) <= 1e-6
+    for fld in (fsim.FIELD_VELOCITY, fsim.FIELD_VELOCITY_UPDATE, fsim.FIELD_PRESSURE):
+        x, xa = a.field(fld)
+        y, ya = b.field(fld)
+        assert np.array_equal(xa, ya)
+        assert rel_l2(x, y) <= 1e-6
+    a.close()
+    b.close()
+
+
+def test_step_deterministic():
+    """Two runs of one step from the same state: topology and positions are
+    bit-identical; the PCG (fixed-order reductions) is deterministic given the
+    same divergence; P2G float sums may reorder (shared-memory atomics), so
+    fields are compared at the bar."""
+    cfg = SCENES[1]
+    orc = make_oracle(cfg["n"], cfg["scene"], noise=_noise(cfg["n"]))
+    prm = fsim.pcg_params(fsim.PCG_ABSOLUTE, fsim.PREC_FP32, 1500,
+                          threshold=float(np.float32(cfg["n"] ** 3) * np.float32(0.5e-8)))
+    outs = []
+    for _ in range(2):
+        sim = make_gpu(orc)
+        st = sim.step(0.01, prm)
+        p, v, g = sim.download_particles()
+        x, _ = sim.field(fsim.FIELD_PRESSURE)
+        m, _ = sim.marker()
+        outs.append((p, v, g, x, m, st.pcg.iterations))
+        sim.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    assert np.array_equal(outs[0][4], outs[1][4])
+    assert rel_l2(outs[0][1], outs[1][1]) <= FIELD_RTOL
+    assert rel_l2(outs[0][3], outs[1][3]) <= FIELD_RTOL

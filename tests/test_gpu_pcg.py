@@ -1,0 +1,108 @@
+"""GPU PCG parity and precision modes (PCGDriver::Solve restated).
+
+All solves run on the divergence and marker of the same replayed step, so
+GPU and oracle see the same system up to the divergence's rounding (<=1e-6).
+"""
+import numpy as np
+import pytest
+
+import fsim
+from _util import make_gpu, make_oracle, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _prepared(n=32, scene="dam_break", noise=True):
+    orc = make_oracle(n, scene, noise=0.3 * n if noise else 0.0)
+    sim = make_gpu(orc)
+    dt = 0.01
+    for o in (orc, sim):
+        o.move_particles(dt)
+        o.clear_grid()
+        o.transfer_particles_to_grid()
+        o.apply_boundary_conditions()
+        o.save_grid_velocities()
+        o.add_gravity(dt)
+        o.apply_boundary_conditions()
+        o.compute_divergence()
+    return orc, sim
+
+
+def _pressures(sim, orc):
+    a, aa = sim.field(fsim.FIELD_PRESSURE)
+    b, ba = orc.field(4)
+    assert np.array_equal(aa, ba), "pressure active set (FLUID cells) differs"
+    return a, b
+
+
+def test_fp32_fixed_iterations_track_oracle():
+    orc, sim = _prepared()
+    for it in (1, 5, 25):
+        st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_FIXED, fsim.PREC_FP32, it))
+        ost = orc.pcg_solve(mode=2, precision=0, max_iterations=it)
+        assert st.iterations == it and ost.iterations == it
+        a, b = _pressures(sim, orc)
+        # same algorithm; only the dot-product summation order differs
+        assert rel_l2(a, b) <= 1e-5, it
+        assert abs(st.rr - ost.rr) <= 1e-3 * ost.rr + 1e-30
+    sim.close()
+
+
+def test_reference_absolute_rule():
+    orc, sim = _prepared()
+    prm = sim.default_pcg_params()
+    assert prm.mode == fsim.PCG_ABSOLUTE and prm.max_iterations == 1500
+    assert prm.threshold == float(np.float32(32 ** 3) * np.float32(0.5e-8))
+    st = sim.pcg_solve(prm)
+    ost = orc.pcg_solve(mode=0, precision=0, max_iterations=1500, threshold=prm.threshold)
+    assert st.status == 0 and ost.status == 0
+    assert abs(st.iterations - ost.iterations) <= 2
+    assert st.rr < prm.threshold
+    a, b = _pressures(sim, orc)
+    assert rel_l2(a, b) <= 1e-4
+    sim.close()
+
+
+def test_mixed_matches_fp64_oracle():
+    orc, sim = _prepared()
+    ost = orc.pcg_solve(mode=1, precision=2, max_iterations=20000, tol=1e-14)
+    x64 = orc.pressure_f64()
+    st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 2000,
+                                       tolerance=1e-9, inner_tolerance=1e-3))
+    assert st.status == 0 and st.refinements >= 2
+    a, _ = sim.field(fsim.FIELD_PRESSURE)
+    assert rel_l2(a, x64) <= 1e-6
+    assert np.sqrt(st.rr / st.bb) <= 1e-9
+    sim.close()
+
+
+def test_fp64_matches_fp64_oracle():
+    orc, sim = _prepared(n=24, scene="sphere_drop")
+    ost = orc.pcg_solve(mode=1, precision=2, max_iterations=20000, tol=1e-12)
+    st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP64, 20000, tolerance=1e-12))
+    assert st.status == 0 and ost.status == 0
+    assert abs(st.iterations - ost.iterations) <= 2
+    a, _ = sim.field(fsim.FIELD_PRESSURE)
+    assert rel_l2(a, orc.pressure_f64()) <= 1e-7
+    sim.close()
+
+
+def test_relative_not_converged_status():
+    orc, sim = _prepared()
+    st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 3, tolerance=1e-12))
+    assert st.status == fsim.ERR_NOT_CONVERGED and st.iterations == 3
+    sim.close()
+
+
+def test_empty_fluid_solve():
+    n = 16
+    g, f = fsim.physical_gravity(n)
+    with fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f) as sim:
+        pos = np.array([[8.5, 8.5, 8.5]], np.float32)
+        z = np.zeros_like(pos)
+        sim.upload_particles(pos, z, z)
+        sim.transfer_particles_to_grid()
+        sim.apply_boundary_conditions()
+        sim.compute_divergence()
+        st = sim.pcg_solve(sim.default_pcg_params())
+        assert st.status == 0
