@@ -47,10 +47,12 @@ WORKLOADS = {
     "sphere_pool_1024": dict(n=1024, scene="sphere_pool"),
 }
 
-# Algorithmic HBM bytes per fluid cell (DOF) per launch of each PCG kernel:
-#   pcg_spmv:   read r, p_old (8) + flags (1); write p, Ap (8)        = 17 B
-#   pcg_update: read x, p, r, Ap (16) + flags (1); write x, r (8)     = 25 B
-ALG_BYTES = {"pcg_spmv": 17, "pcg_update": 25, "pcg_spmv_mixed": 17, "pcg_update_mixed": 25}
+# Algorithmic HBM bytes per unknown (fluid cell) per launch of each PCG kernel
+# (Ap is never stored; z = r/diag is recomputed):
+#   pcg_spmv:   read r, p_{j-1} (8) + flags (1); write p_j (4)        = 13 B
+#   pcg_update: read p_j, x, r (12) + flags (1); write x, r (8)       = 21 B
+ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update_mixed": 21,
+             "pcg_spmv_f64": 25, "pcg_update_f64": 41}
 
 
 def peaks():
@@ -163,8 +165,6 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         st = sim.step(next_dt(), prm)
         inv = st.next_inv_speed
-    sim.set_profiling(True)
-    sim.reset_kernel_times()
     launches0 = sim.launch_count()
     iters, rows = [], []
     barrier()
@@ -182,8 +182,24 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
     barrier()
     ms = ev0.elapsed_time(ev1)
-    kt = sim.kernel_times()
     launches = sim.launch_count() - launches0
+    # per-kernel CUDA-event times on the library's stream (a second pass, so
+    # the events do not perturb the timed steps above)
+    sim.set_profiling(True)
+    sim.reset_kernel_times()
+    piters, prows = [], []
+    t1 = torch.cuda.Event(enable_timing=True)
+    t2 = torch.cuda.Event(enable_timing=True)
+    t1.record(stream)
+    for _ in range(max(1, min(args.steps, args.profile_steps))):
+        st = sim.step(next_dt(), prm)
+        inv = st.next_inv_speed
+        piters.append(st.pcg.iterations)
+        prows.append(st.pcg.n_rows)
+    t2.record(stream)
+    torch.cuda.synchronize()
+    prof_ms = t1.elapsed_time(t2)
+    kt = sim.kernel_times()
     sim.set_profiling(False)
     if world > 1:
         t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
@@ -223,6 +239,7 @@ def run_gpu(args, rank, world):
     barrier()
     sim.close()
     return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, clocks=clk.summary(),
+                piters=piters, prows=prows, prof_ms=prof_ms,
                 n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms,
                 e2e_bytes=36 * n_particles)
 
@@ -234,13 +251,14 @@ def roofline(res):
         return None
     top = max(kt.items(), key=lambda kv: kv[1][0])
     name, (tot_ms, nl) = top
-    total_iters = sum(res["iters"])
-    # bytes of each working launch = per-DOF bytes x that step's unknowns
+    total_iters = sum(res["piters"])
+    # bytes of each working launch = per-unknown bytes x that step's unknowns
     out = {"bound": "hbm", "kernel": name, "peak": peak, "peak_source": src, "unit": "GB/s",
-           "share_of_step": tot_ms / res["ms"] if res["ms"] > 0 else None, "traffic": None}
-    if name in ALG_BYTES and res["n_fluid"]:
-        alg = ALG_BYTES[name] * res["n_fluid"]  # per working launch (mean unknowns)
-        tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["rows"], res["iters"]))
+           "share_of_step": tot_ms / res["prof_ms"] if res["prof_ms"] > 0 else None,
+           "traffic": None}
+    if name in ALG_BYTES and res["prows"]:
+        alg = ALG_BYTES[name] * float(np.mean(res["prows"]))  # per working launch
+        tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["prows"], res["piters"]))
         achieved = tot_bytes / (tot_ms * 1e-3) / 1e9
         out.update(achieved=achieved, frac=achieved / peak,
                    alg_bytes_per_launch=alg, working_launches=total_iters, launches=nl)
@@ -249,8 +267,15 @@ def roofline(res):
     return out
 
 
-def cpu_sample(args):
-    """The oracle on a bounded sample of the same workload (single thread)."""
+def cpu_sample(args, iters_per_step=None):
+    """The oracle on a bounded sample of the same workload (single thread).
+
+    Times the first step of the scene stage by stage.  With iters_per_step
+    given, the PCG runs only args.cpu_pcg_iters iterations: its setup and
+    per-iteration cost are measured and the step time is extrapolated to
+    iters_per_step iterations (the GPU's mean for its timed steps).  Without
+    it the PCG runs to the workload's own stopping rule.
+    """
     import fsim
     from oracle.oracle import OracleSim
 
@@ -259,20 +284,47 @@ def cpu_sample(args):
     g, f = fsim.physical_gravity(n)
     orc = OracleSim((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8)
     orc.seed(fsim.scene_passes(wl["scene"], n), seed=0)
-    t_in = 0.0
-    times, iters = [], []
-    budget = args.cpu_budget
-    t_start = time.perf_counter()
-    while True:
-        inv = orc.cfl()
-        dt, t_in = fsim_dt(inv, t_in)
-        t0 = time.perf_counter()
-        st = orc.step(dt, mode=1, precision=0, max_iterations=args.max_iterations, tol=args.tol)
-        times.append(time.perf_counter() - t0)
-        iters.append(st.iterations)
-        if time.perf_counter() - t_start > budget or len(times) >= args.cpu_steps:
-            break
-    return times, iters, orc.particle_count()
+    npart = orc.particle_count()
+    dt, _ = fsim_dt(orc.cfl(), 0.0)
+    clock = time.perf_counter
+    t0 = clock()
+    orc.move_particles(dt)
+    orc.clear_grid()
+    orc.transfer_particles_to_grid()
+    orc.apply_boundary_conditions()
+    orc.save_grid_velocities()
+    orc.delete_outside_particles()
+    orc.reinitialize_phi()
+    orc.add_gravity(dt)
+    orc.apply_boundary_conditions()
+    orc.compute_divergence()
+    t_pre = clock() - t0
+    if iters_per_step is None:
+        t0 = clock()
+        st = orc.pcg_solve(mode=1, precision=0, max_iterations=args.max_iterations, tol=args.tol)
+        t_pcg = clock() - t0
+        iters = st.iterations
+        how = f"{iters} PCG iterations run in full"
+    else:
+        m = args.cpu_pcg_iters
+        t0 = clock()
+        orc.pcg_solve(mode=2, precision=0, max_iterations=0)
+        t_setup = clock() - t0
+        t0 = clock()
+        orc.pcg_solve(mode=2, precision=0, max_iterations=m)
+        t_m = clock() - t0
+        per_it = max(t_m - t_setup, 0.0) / m
+        iters = iters_per_step
+        t_pcg = t_setup + per_it * iters
+        how = (f"PCG setup + {m} iterations timed ({per_it * 1e3:.1f} ms/iteration), "
+               f"extrapolated to {iters:.1f} iterations/step")
+    t0 = clock()
+    orc.update_velocity_from_pressure()
+    orc.get_velocity_update()
+    orc.update_particles_from_grid()
+    t_post = clock() - t0
+    t_step = t_pre + t_pcg + t_post
+    return t_step, npart, how
 
 
 def fsim_dt(inv, t_in):
@@ -295,8 +347,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--max-iterations", type=int, default=1500)
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-steps", type=int, default=1)
-    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    ap.add_argument("--cpu-pcg-iters", type=int, default=40)
+    ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
 
@@ -312,21 +364,19 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # Each step is one full reference FLIP step (~tens of seconds at
-        # 256^3); the run is capped at 1 warm-up + 2 timed steps so that it
-        # ends within a few minutes.
-        args.cpu_steps = 1 + min(args.steps, 2) if args.warmup > 0 else min(args.steps, 2)
-        args.cpu_budget = 1e9
-        times, iters, npart = cpu_sample(args)
-        timed = times[1:] if args.warmup > 0 and len(times) > 1 else times
-        v = len(timed) / sum(timed)
+        # One full reference FLIP step (the first step of the scene, PCG run
+        # to the workload's stopping rule) is the timed sample: about two
+        # minutes of single-thread CPU work at 256^3.
+        t_step, npart, how = cpu_sample(args, None)
+        v = 1.0 / t_step
         line = {"impl": "reference", "metric": "FLIP steps/s", "value": v, "unit": "steps/s",
-                "n_gpus": args.gpus, "steps": len(timed), "warmup": len(times) - len(timed),
-                "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * t_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                 "sample": f"{len(timed)} full steps of {args.workload} "
-                                           f"({npart} particles, PCG iters {iters})"},
+                                 "sample": f"first step of {args.workload} ({npart} particles; "
+                                           f"{how}); oracle restatement of the reference CPU "
+                                           f"path, one thread (one partition, TBB at 1 thread)"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -353,11 +403,11 @@ def main():
             "kernels_ms": {k: round(v[0], 3) for k, v in sorted(res["kt"].items(),
                                                                 key=lambda kv: -kv[1][0])}}
     if not args.no_cpu:
-        times, iters, npart = cpu_sample(args)
-        v = len(times) / sum(times)
-        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                "sample": f"first {len(times)} step(s) of {args.workload} from "
-                                          f"rest ({npart} particles, PCG iters {iters})"}
+        t_step, npart, how = cpu_sample(args, float(np.mean(res["iters"])))
+        line["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": 1,
+                                "kind": "port",
+                                "sample": f"first step of {args.workload} ({npart} particles), "
+                                          f"stages timed on one thread; {how}"}
     print(json.dumps(line))
 
 

@@ -29,7 +29,6 @@ struct G2PArgs {
   const uint32_t* vold_on;
   LeafMap lm;
   float flip;
-  int check_dead;
 };
 
 __device__ __forceinline__ int side(int t) { return t < 0 ? -1 : (t > 7 ? 1 : 0); }
@@ -74,9 +73,12 @@ __global__ void __launch_bounds__(256) k_g2p(const __grid_constant__ G2PArgs a) 
   const int64_t cap = a.cap;
   float* P = a.part;
   for (uint32_t q = lr.x + tid; q < lr.y; q += 256) {
-    if (a.check_dead && a.keys[q] == kDeadKey) continue;
+    const uint32_t key = a.keys[q];
+    if (key == kDeadKey) continue;
     const float p[3] = {P[q], P[cap + q], P[2 * cap + q]};
-    const int cc[3] = {int(floorf(p[0])), int(floorf(p[1])), int(floorf(p[2]))};
+    // the cell the particle is binned in (as the reference's per-cell list)
+    const int vx = int(key & 511u);
+    const int cc[3] = {org[0] + (vx >> 6), org[1] + ((vx >> 3) & 7), org[2] + (vx & 7)};
     float pv[3] = {P[3 * cap + q], P[4 * cap + q], P[5 * cap + q]};
     float vi[3], di[3];
 #pragma unroll
@@ -129,7 +131,6 @@ int launch_g2p(fsim_sim* s) {
   a.vold_on = s->vold_on;
   a.lm = s->lm;
   a.flip = s->cfg.flip_factor;
-  a.check_dead = s->deleted_outside ? 1 : 0;
   FSIM_LAUNCH(s, "g2p", k_g2p, s->n_pleaf, 256, 0, a);
   return FSIM_OK;
 }

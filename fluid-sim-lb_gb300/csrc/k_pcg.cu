@@ -19,8 +19,9 @@
 //           iteration and sets the stop flag.
 // HBM bytes per unknown per iteration: spmv reads r, p_{j-1}, flags and
 // writes p_j (13 B); update reads p_j, x, r, flags and writes x, r (21 B).
-// Each CTA stages one leaf's p plus its six face halos in shared memory;
-// every thread owns one z-quad of 4 cells (float4 / double2 accesses).  Kernels launched after the stop flag is set return at
+// Each warp owns one leaf: a lane holds two z-columns of 8 cells in
+// registers, neighbours come from warp shuffles and only the six leaf faces
+// are read from the neighbour leaves.  Kernels launched after the stop flag is set return at
 // once, so the host polls the flag only between chunks of iterations.
 //
 // Precision modes: FP32 (reference: fp32 vectors, fp32 dots), MIXED (fp32
@@ -36,7 +37,10 @@ namespace fsim {
 
 namespace {
 
-constexpr int kThreads = 128;  // 4 cells per thread, one 8^3 leaf per pass
+constexpr int kThreads = 256;  // 8 warps; the hot kernels give each warp one leaf
+#ifndef FSIM_PCG_MINB
+#define FSIM_PCG_MINB 1  // min resident CTAs per SM requested from ptxas
+#endif
 
 // Jacobi: T(1.0/diag) (diag 0 gives inf, as 1.0/0 does in the reference)
 __constant__ float c_invf[8] = {__builtin_inff(), 1.0f, 0.5f, float(1.0 / 3.0),
@@ -270,131 +274,225 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
   }
 }
 
-// ---- 4-cell vector access: each thread owns cells v0..v0+3 (one z quad)
+// ---- column-blocked leaf access -------------------------------------------
+// One warp owns one 8^3 leaf.  Lane L owns the two z-columns (cx, cy) and
+// (cx+4, cy) with cx = L>>3, cy = L&7; a column is 8 contiguous cells
+// (offset x*64 + y*8, 32 B of floats), so the z-neighbours are registers,
+// the y-neighbours are lanes L-1 / L+1 and the x-neighbours lanes L-8 / L+8
+// (or L-24 / L+24 between the two column sets) -- all warp shuffles.  Only
+// the six leaf faces come from the neighbour leaves.  No shared memory and
+// no CTA barrier in the hot loop.
 template <typename T>
-struct Quad {
-  T v[4];
+struct Col {
+  T v[8];
 };
-__device__ __forceinline__ Quad<float> ld4(const float* p, int64_t o) {
-  const float4 t = *reinterpret_cast<const float4*>(p + o);
-  return Quad<float>{{t.x, t.y, t.z, t.w}};
-}
-__device__ __forceinline__ Quad<double> ld4(const double* p, int64_t o) {
-  const double2 a = *reinterpret_cast<const double2*>(p + o);
-  const double2 b = *reinterpret_cast<const double2*>(p + o + 2);
-  return Quad<double>{{a.x, a.y, b.x, b.y}};
-}
-__device__ __forceinline__ void st4(float* p, int64_t o, const Quad<float>& q) {
-  *reinterpret_cast<float4*>(p + o) = make_float4(q.v[0], q.v[1], q.v[2], q.v[3]);
-}
-__device__ __forceinline__ void st4(double* p, int64_t o, const Quad<double>& q) {
-  *reinterpret_cast<double2*>(p + o) = make_double2(q.v[0], q.v[1]);
-  *reinterpret_cast<double2*>(p + o + 2) = make_double2(q.v[2], q.v[3]);
-}
 
-// Halo cell h in [0,384): face = h/64 (0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z);
-// returns the neighbour-table index and the voxel inside that neighbour.
-__device__ __forceinline__ void halo_cell(int h, int& q, int& vox) {
-  const int face = h >> 6, u = (h >> 3) & 7, w = h & 7;
-  const int d = (face & 1) ? 1 : -1;
-  const int e = d < 0 ? 7 : 0;
-  if (face < 2) { q = (d + 1) * 9 + 4; vox = (e << 6) | (u << 3) | w; }
-  else if (face < 4) { q = 9 + (d + 1) * 3 + 1; vox = (u << 6) | (e << 3) | w; }
-  else { q = 12 + (d + 1); vox = (u << 6) | (w << 3) | e; }
+__device__ __forceinline__ void ldcol(const float* __restrict__ p, int64_t o, Col<float>& c) {
+  const float4 a = __ldcg(reinterpret_cast<const float4*>(p + o));
+  const float4 b = __ldcg(reinterpret_cast<const float4*>(p + o + 4));
+  c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
+  c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
 }
-
-// A*p for the four cells v0..v0+3 from the staged leaf+halo tile pn, summed
-// in the column order of the reference's rows: -x,-y,-z, diag, +z,+y,+x.
-template <typename T>
-__device__ __forceinline__ void stencil4(const T* pn, int v0, uint32_t f4, T out[4]) {
-  const int cx = v0 >> 6, cy = (v0 >> 3) & 7, cz0 = v0 & 7;
+__device__ __forceinline__ void ldcol(const double* __restrict__ p, int64_t o, Col<double>& c) {
 #pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const int v = v0 + c, cz = cz0 + c;
-    const uint8_t f = uint8_t(f4 >> (8 * c));
-    T acc = T(0);
-    if (f & 1) {
-      const T mx = cx > 0 ? pn[v - 64] : pn[512 + 0 * 64 + cy * 8 + cz];
-      const T px = cx < 7 ? pn[v + 64] : pn[512 + 1 * 64 + cy * 8 + cz];
-      const T my = cy > 0 ? pn[v - 8] : pn[512 + 2 * 64 + cx * 8 + cz];
-      const T py = cy < 7 ? pn[v + 8] : pn[512 + 3 * 64 + cx * 8 + cz];
-      const T mz = cz > 0 ? pn[v - 1] : pn[512 + 4 * 64 + cx * 8 + cy];
-      const T pz = cz < 7 ? pn[v + 1] : pn[512 + 5 * 64 + cx * 8 + cy];
-      acc = tsub(acc, mx);
-      acc = tsub(acc, my);
-      acc = tsub(acc, mz);
-      acc = tadd(acc, tmul(T(flag_diag(f)), pn[v]));
-      acc = tsub(acc, pz);
-      acc = tsub(acc, py);
-      acc = tsub(acc, px);
-    }
-    out[c] = acc;
+  for (int k = 0; k < 4; ++k) {
+    const double2 a = __ldcg(reinterpret_cast<const double2*>(p + o + 2 * k));
+    c.v[2 * k] = a.x;
+    c.v[2 * k + 1] = a.y;
   }
+}
+__device__ __forceinline__ void stcol(float* __restrict__ p, int64_t o, const Col<float>& c) {
+  *reinterpret_cast<float4*>(p + o) = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
+  *reinterpret_cast<float4*>(p + o + 4) = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
+}
+__device__ __forceinline__ void stcol(double* __restrict__ p, int64_t o, const Col<double>& c) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    *reinterpret_cast<double2*>(p + o + 2 * k) = make_double2(c.v[2 * k], c.v[2 * k + 1]);
+}
+__device__ __forceinline__ uint2 ldflags(const uint8_t* __restrict__ f, int64_t o) {
+  return __ldcg(reinterpret_cast<const uint2*>(f + o));
+}
+__device__ __forceinline__ uint8_t fbyte(uint2 f, int z) {
+  return uint8_t((z < 4 ? f.x : f.y) >> (8 * (z & 3)));
+}
+
+// p = z + beta p_old with z = r/diag (p = z at the first iteration); 0 off-fluid
+template <typename T>
+__device__ __forceinline__ T pnew_cell(uint8_t f, T r, T po, T beta, bool first) {
+  if (!(f & 1)) return T(0);
+  const T z = tmul(inv_diag<T>(f), r);
+  return first ? z : tadd(z, tmul(beta, po));
+}
+
+// p_new of a whole neighbour column (spmv: from r, p_old, flags)
+template <typename T>
+__device__ __forceinline__ void pnew_column(const PcgArgs& a, int ns, int vox0, T beta, bool first,
+                                            const T* r, const T* pold, Col<T>& out) {
+  if (ns < 0 || ns >= a.n_pleaf) {
+#pragma unroll
+    for (int z = 0; z < 8; ++z) out.v[z] = T(0);
+    return;
+  }
+  const int64_t o = int64_t(ns) * 512 + vox0;
+  const uint2 f = ldflags(a.flags, o);
+  Col<T> rc, pc;
+  ldcol(r, o, rc);
+  if (!first) ldcol(pold, o, pc);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) out.v[z] = pnew_cell<T>(fbyte(f, z), rc.v[z], first ? T(0) : pc.v[z],
+                                                     beta, first);
+}
+
+// p_new of one neighbour cell (z faces)
+template <typename T>
+__device__ __forceinline__ T pnew_one(const PcgArgs& a, int ns, int vox, T beta, bool first,
+                                      const T* r, const T* pold) {
+  if (ns < 0 || ns >= a.n_pleaf) return T(0);
+  const int64_t o = int64_t(ns) * 512 + vox;
+  const uint8_t f = __ldcg(a.flags + o);
+  return pnew_cell<T>(f, __ldcg(r + o), first ? T(0) : __ldcg(pold + o), beta, first);
+}
+
+template <typename T>
+__device__ __forceinline__ void ld_pcol(const PcgArgs& a, int ns, int vox0, const T* p, Col<T>& out) {
+  if (ns < 0 || ns >= a.n_pleaf) {
+#pragma unroll
+    for (int z = 0; z < 8; ++z) out.v[z] = T(0);
+    return;
+  }
+  ldcol(p, int64_t(ns) * 512 + vox0, out);
+}
+
+template <typename T>
+__device__ __forceinline__ T ld_pone(const PcgArgs& a, int ns, int vox, const T* p) {
+  if (ns < 0 || ns >= a.n_pleaf) return T(0);
+  return __ldcg(p + int64_t(ns) * 512 + vox);
+}
+
+__device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// The six face-neighbour slots of leaf s, gathered by lanes 0..5 and
+// broadcast: 0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z.
+__device__ __forceinline__ void face_slots(const int32_t* nb, int lane, int out[6]) {
+  int q = 13;
+  if (lane == 0) q = 4; else if (lane == 1) q = 22; else if (lane == 2) q = 10;
+  else if (lane == 3) q = 16; else if (lane == 4) q = 12; else if (lane == 5) q = 14;
+  const int mine = (lane < 6) ? __ldg(nb + q) : -1;
+#pragma unroll
+  for (int f = 0; f < 6; ++f) out[f] = __shfl_sync(0xffffffffu, mine, f);
+}
+
+// A p at height z of the lane's two columns P0 (x = cx) and P1 (x = cx+4),
+// summed in the reference's column order (-x,-y,-z, diag, +z,+y,+x).  A lane
+// needs at most one x-face column xh (the -x face when cx == 0, the +x face
+// when cx == 3) and one y-face pair yh0/yh1 (the -y face when cy == 0, the
+// +y face when cy == 7); zm*/zp* are the -z / +z face cells.
+template <typename T>
+__device__ __forceinline__ void stencil_z(int z, const Col<T>& P0, const Col<T>& P1, uint8_t g0,
+                                          uint8_t g1, const Col<T>& xh, const Col<T>& yh0,
+                                          const Col<T>& yh1, T zm0, T zp0, T zm1, T zp1,
+                                          int lane, T& a0, T& a1) {
+  const int cx = lane >> 3, cy = lane & 7;
+  const T s_xp0 = (cx == 0) ? P1.v[z] : P0.v[z];
+  const T s_xm1 = (cx == 3) ? P0.v[z] : P1.v[z];
+  const T a_xm0 = shfl(P0.v[z], (lane - 8) & 31);
+  const T a_xp0 = shfl(s_xp0, cx < 3 ? lane + 8 : lane - 24);
+  const T a_xm1 = shfl(s_xm1, cx > 0 ? lane - 8 : lane + 24);
+  const T a_xp1 = shfl(P1.v[z], (lane + 8) & 31);
+  const T a_ym0 = shfl(P0.v[z], (lane - 1) & 31), a_yp0 = shfl(P0.v[z], (lane + 1) & 31);
+  const T a_ym1 = shfl(P1.v[z], (lane - 1) & 31), a_yp1 = shfl(P1.v[z], (lane + 1) & 31);
+  const T xm_0 = cx == 0 ? xh.v[z] : a_xm0;
+  const T xp_1 = cx == 3 ? xh.v[z] : a_xp1;
+  const T ym_0 = cy == 0 ? yh0.v[z] : a_ym0, yp_0 = cy == 7 ? yh0.v[z] : a_yp0;
+  const T ym_1 = cy == 0 ? yh1.v[z] : a_ym1, yp_1 = cy == 7 ? yh1.v[z] : a_yp1;
+  const T zm_0 = z == 0 ? zm0 : P0.v[(z + 7) & 7], zp_0 = z == 7 ? zp0 : P0.v[(z + 1) & 7];
+  const T zm_1 = z == 0 ? zm1 : P1.v[(z + 7) & 7], zp_1 = z == 7 ? zp1 : P1.v[(z + 1) & 7];
+  T acc = T(0);
+  if (g0 & 1) {
+    acc = tsub(acc, xm_0);
+    acc = tsub(acc, ym_0);
+    acc = tsub(acc, zm_0);
+    acc = tadd(acc, tmul(T(flag_diag(g0)), P0.v[z]));
+    acc = tsub(acc, zp_0);
+    acc = tsub(acc, yp_0);
+    acc = tsub(acc, a_xp0);
+  }
+  a0 = acc;
+  acc = T(0);
+  if (g1 & 1) {
+    acc = tsub(acc, a_xm1);
+    acc = tsub(acc, ym_1);
+    acc = tsub(acc, zm_1);
+    acc = tadd(acc, tmul(T(flag_diag(g1)), P1.v[z]));
+    acc = tsub(acc, zp_1);
+    acc = tsub(acc, yp_1);
+    acc = tsub(acc, xp_1);
+  }
+  a1 = acc;
 }
 
 // p_j = z_j + beta_{j-1} p_{j-1} for the leaf and its face halo (z = r/diag
-// recomputed), then p_j.(A p_j); the last CTA forms alpha_j.  Only p_j is
-// written: the update kernel recomputes A p_j from it instead of storing Ap.
+// recomputed, never stored), then p_j.(A p_j); the last CTA forms alpha_j.
+// Only p_j is written: the update kernel recomputes A p_j from it.
 template <typename T, int DM>
-__global__ void __launch_bounds__(kThreads, 12) k_pcg_spmv(const __grid_constant__ PcgArgs a) {
-  __shared__ T pn[512 + 384];
+__global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_spmv(const __grid_constant__ PcgArgs a) {
   const PcgScalars* sc = a.sc;
   if (sc->done) return;
   const int it = sc->iter;
+  const bool first = it == 0;
   const T beta = T(sc->beta);
   const T* r = static_cast<const T*>(a.r);
   const T* pold = static_cast<const T*>((it & 1) ? a.p0 : a.p1);
   T* pnew = static_cast<T*>((it & 1) ? a.p1 : a.p0);
-  const uint32_t* flags4 = reinterpret_cast<const uint32_t*>(a.flags);
-  const int v0 = threadIdx.x * 4;
+  const int lane = threadIdx.x & 31;
+  const int cx = lane >> 3, cy = lane & 7;
+  const int c0 = (cx << 6) | (cy << 3), c1 = ((cx + 4) << 6) | (cy << 3);
+  const int wpb = kThreads / 32;
   Dot<DM> dp;
-  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
-    const int32_t* nb = a.nbr + int64_t(s) * 27;
-    const int64_t o = int64_t(s) * 512 + v0;
-    const uint32_t f4 = flags4[o >> 2];
-    const Quad<T> rq = ld4(r, o);
-    Quad<T> pq;
-    if (it > 0) pq = ld4(pold, o);
-    // halo values first (independent loads in flight)
-    T hv[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int h = threadIdx.x + k * kThreads;
-      int q, vox;
-      halo_cell(h, q, vox);
-      const int ns = nb[q];
-      T pv = T(0);
-      if (ns >= 0 && ns < a.n_pleaf) {
-        const int64_t u = int64_t(ns) * 512 + vox;
-        const uint8_t f = a.flags[u];
-        const T z = tmul(inv_diag<T>(f), r[u]);
-        pv = (it == 0) ? z : tadd(z, tmul(beta, pold[u]));
-        if (!(f & 1)) pv = T(0);
-      }
-      hv[k] = pv;
+  for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < a.n_pleaf; s += gridDim.x * wpb) {
+    int fs[6];
+    face_slots(a.nbr + int64_t(s) * 27, lane, fs);
+    const int64_t base = int64_t(s) * 512;
+    const uint2 f0 = ldflags(a.flags, base + c0), f1 = ldflags(a.flags, base + c1);
+    Col<T> r0, r1, q0, q1;
+    ldcol(r, base + c0, r0);
+    ldcol(r, base + c1, r1);
+    if (!first) {
+      ldcol(pold, base + c0, q0);
+      ldcol(pold, base + c1, q1);
     }
-    __syncthreads();  // previous leaf's stencil reads of pn are done
-    Quad<T> out;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const uint8_t f = uint8_t(f4 >> (8 * c));
-      T pv = T(0);
-      if (f & 1) {
-        const T z = tmul(inv_diag<T>(f), rq.v[c]);
-        pv = (it == 0) ? z : tadd(z, tmul(beta, pq.v[c]));
-      }
-      out.v[c] = pv;
-      pn[v0 + c] = pv;
+    // face halos (p_new computed from the neighbour's r, p_old, flags)
+    Col<T> xh, yh0, yh1;
+    if (cx == 0 || cx == 3)
+      pnew_column(a, cx == 0 ? fs[0] : fs[1], ((cx == 0 ? 7 : 0) << 6) | (cy << 3), beta, first,
+                  r, pold, xh);
+    if (cy == 0 || cy == 7) {
+      const int ns = cy == 0 ? fs[2] : fs[3], yy = (cy == 0 ? 7 : 0) << 3;
+      pnew_column(a, ns, (cx << 6) | yy, beta, first, r, pold, yh0);
+      pnew_column(a, ns, ((cx + 4) << 6) | yy, beta, first, r, pold, yh1);
     }
-    st4(pnew, o, out);
+    const T zm0 = pnew_one(a, fs[4], c0 | 7, beta, first, r, pold);
+    const T zm1 = pnew_one(a, fs[4], c1 | 7, beta, first, r, pold);
+    const T zp0 = pnew_one(a, fs[5], c0, beta, first, r, pold);
+    const T zp1 = pnew_one(a, fs[5], c1, beta, first, r, pold);
+    Col<T> P0, P1;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) pn[512 + threadIdx.x + k * kThreads] = hv[k];
-    __syncthreads();
-    T ap[4];
-    stencil4(pn, v0, f4, ap);
+    for (int z = 0; z < 8; ++z) {
+      P0.v[z] = pnew_cell<T>(fbyte(f0, z), r0.v[z], first ? T(0) : q0.v[z], beta, first);
+      P1.v[z] = pnew_cell<T>(fbyte(f1, z), r1.v[z], first ? T(0) : q1.v[z], beta, first);
+    }
+    stcol(pnew, base + c0, P0);
+    stcol(pnew, base + c1, P1);
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
-      if ((f4 >> (8 * c)) & 1u) dp.add(out.v[c], ap[c]);
+    for (int z = 0; z < 8; ++z) {
+      const uint8_t g0 = fbyte(f0, z), g1 = fbyte(f1, z);
+      T a0, a1;
+      stencil_z<T>(z, P0, P1, g0, g1, xh, yh0, yh1, zm0, zp0, zm1, zp1, lane, a0, a1);
+      if (g0 & 1) dp.add(P0.v[z], a0);
+      if (g1 & 1) dp.add(P1.v[z], a1);
+    }
   }
   double v[1] = {dp.value()};
   double tot[1];
@@ -410,11 +508,10 @@ __global__ void __launch_bounds__(kThreads, 12) k_pcg_spmv(const __grid_constant
   }
 }
 
-// Ap = A p_j recomputed from p_j (leaf + face halo); x += alpha p;
+// A p_j recomputed from p_j (leaf + face halo); x += alpha p;
 // r -= alpha Ap; r.r and r.z; the last CTA forms beta and the stop test.
 template <typename T, int DM>
-__global__ void __launch_bounds__(kThreads, 12) k_pcg_update(const __grid_constant__ PcgArgs a) {
-  __shared__ T pn[512 + 384];
+__global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_update(const __grid_constant__ PcgArgs a) {
   const PcgScalars* sc = a.sc;
   if (sc->done) return;
   const int it = sc->iter;
@@ -423,46 +520,55 @@ __global__ void __launch_bounds__(kThreads, 12) k_pcg_update(const __grid_consta
   const T* p = static_cast<const T*>((it & 1) ? a.p1 : a.p0);
   T* x = static_cast<T*>(a.x);
   T* r = static_cast<T*>(a.r);
-  const uint32_t* flags4 = reinterpret_cast<const uint32_t*>(a.flags);
-  const int v0 = threadIdx.x * 4;
+  const int lane = threadIdx.x & 31;
+  const int cx = lane >> 3, cy = lane & 7;
+  const int c0 = (cx << 6) | (cy << 3), c1 = ((cx + 4) << 6) | (cy << 3);
+  const int wpb = kThreads / 32;
   Dot<DM> drr, drz;
-  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
-    const int32_t* nb = a.nbr + int64_t(s) * 27;
-    const int64_t o = int64_t(s) * 512 + v0;
-    const uint32_t f4 = flags4[o >> 2];
-    const Quad<T> pq = ld4(p, o);
-    const Quad<T> xq = ld4(x, o);
-    const Quad<T> rq = ld4(r, o);
-    T hv[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      int q, vox;
-      halo_cell(threadIdx.x + k * kThreads, q, vox);
-      const int ns = nb[q];
-      hv[k] = (ns >= 0 && ns < a.n_pleaf) ? p[int64_t(ns) * 512 + vox] : T(0);
+  for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < a.n_pleaf; s += gridDim.x * wpb) {
+    int fs[6];
+    face_slots(a.nbr + int64_t(s) * 27, lane, fs);
+    const int64_t base = int64_t(s) * 512;
+    const uint2 f0 = ldflags(a.flags, base + c0), f1 = ldflags(a.flags, base + c1);
+    Col<T> P0, P1, x0, x1, r0, r1;
+    ldcol(p, base + c0, P0);
+    ldcol(p, base + c1, P1);
+    Col<T> xh, yh0, yh1;
+    if (cx == 0 || cx == 3)
+      ld_pcol(a, cx == 0 ? fs[0] : fs[1], ((cx == 0 ? 7 : 0) << 6) | (cy << 3), p, xh);
+    if (cy == 0 || cy == 7) {
+      const int ns = cy == 0 ? fs[2] : fs[3], yy = (cy == 0 ? 7 : 0) << 3;
+      ld_pcol(a, ns, (cx << 6) | yy, p, yh0);
+      ld_pcol(a, ns, ((cx + 4) << 6) | yy, p, yh1);
     }
-    __syncthreads();
+    const T zm0 = ld_pone(a, fs[4], c0 | 7, p), zm1 = ld_pone(a, fs[4], c1 | 7, p);
+    const T zp0 = ld_pone(a, fs[5], c0, p), zp1 = ld_pone(a, fs[5], c1, p);
+    ldcol(x, base + c0, x0);
+    ldcol(x, base + c1, x1);
+    ldcol(r, base + c0, r0);
+    ldcol(r, base + c1, r1);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) pn[v0 + c] = pq.v[c];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) pn[512 + threadIdx.x + k * kThreads] = hv[k];
-    __syncthreads();
-    T ap[4];
-    stencil4(pn, v0, f4, ap);
-    Quad<T> xo, ro;
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      const uint8_t f = uint8_t(f4 >> (8 * c));
-      xo.v[c] = tadd(tmul(alpha, pq.v[c]), xq.v[c]);
-      ro.v[c] = tadd(tmul(nalpha, ap[c]), rq.v[c]);
-      if (f & 1) {
-        const T z = tmul(inv_diag<T>(f), ro.v[c]);
-        drr.add(ro.v[c], ro.v[c]);
-        drz.add(ro.v[c], z);
+    for (int z = 0; z < 8; ++z) {
+      const uint8_t g0 = fbyte(f0, z), g1 = fbyte(f1, z);
+      T a0, a1;
+      stencil_z<T>(z, P0, P1, g0, g1, xh, yh0, yh1, zm0, zp0, zm1, zp1, lane, a0, a1);
+      x0.v[z] = tadd(tmul(alpha, P0.v[z]), x0.v[z]);
+      x1.v[z] = tadd(tmul(alpha, P1.v[z]), x1.v[z]);
+      r0.v[z] = tadd(tmul(nalpha, a0), r0.v[z]);
+      r1.v[z] = tadd(tmul(nalpha, a1), r1.v[z]);
+      if (g0 & 1) {
+        drr.add(r0.v[z], r0.v[z]);
+        drz.add(r0.v[z], tmul(inv_diag<T>(g0), r0.v[z]));
+      }
+      if (g1 & 1) {
+        drr.add(r1.v[z], r1.v[z]);
+        drz.add(r1.v[z], tmul(inv_diag<T>(g1), r1.v[z]));
       }
     }
-    st4(x, o, xo);
-    st4(r, o, ro);
+    stcol(x, base + c0, x0);
+    stcol(x, base + c1, x1);
+    stcol(r, base + c0, r0);
+    stcol(r, base + c1, r1);
   }
   double v[2] = {drr.value(), drz.value()};
   double tot[2];
@@ -537,6 +643,9 @@ template <typename T, int DM>
 int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const char* nm_spmv,
               const char* nm_upd) {
   FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
+  // hot kernels: one warp per leaf, kThreads/32 leaves per CTA
+  const int wgrid = std::max(1, std::min((a.n_pleaf + kThreads / 32 - 1) / (kThreads / 32),
+                                         s->max_blocks));
   int chunk = 8;
   for (;;) {
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
@@ -544,8 +653,8 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     FSIM_CK(s, cudaStreamSynchronize(s->stream));
     if (s->h_sc->done) break;
     for (int c = 0; c < chunk; ++c) {
-      FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), grid, kThreads, 0, a);
-      FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), grid, kThreads, 0, a);
+      FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kThreads, 0, a);
+      FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kThreads, 0, a);
     }
     if (chunk < 64) chunk *= 2;
   }

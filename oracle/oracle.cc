@@ -505,14 +505,20 @@ int64_t orc_seed(orc_sim* s, const orc_seed_pass* passes, int32_t npasses, uint6
           }
         }
   }
-  s->pos.clear(); s->vel_p.clear(); s->gvel.clear();
-  for (size_t c = 0; c < ncell; ++c)
+  // AddParticleToData(i, j, k, pd) files each particle under the cell that
+  // generated it, even when its float position rounds onto the upper face
+  // (org + u == org + 1); StepInGrid rebins by floor(pos) later.
+  s->pos.clear(); s->vel_p.clear(); s->gvel.clear(); s->cell.clear(); s->keys.clear();
+  for (size_t c = 0; c < ncell; ++c) {
+    const int ci = int(c / (size_t(n[1]) * n[2])), cj = int((c / n[2]) % n[1]), ck = int(c % n[2]);
     for (size_t q = 0; q < cp[c].size(); q += 9) {
       for (int d = 0; d < 3; ++d) s->pos.push_back(cp[c][q + d]);
       for (int d = 0; d < 3; ++d) s->vel_p.push_back(cp[c][q + 3 + d]);
       for (int d = 0; d < 3; ++d) s->gvel.push_back(cp[c][q + 6 + d]);
+      s->cell.push_back(ci); s->cell.push_back(cj); s->cell.push_back(ck);
+      s->keys.push_back(s->K.key(ci, cj, ck));
     }
-  recompute_keys(s);
+  }
   reorder_by_key(s);
   return int64_t(s->keys.size());
 }
