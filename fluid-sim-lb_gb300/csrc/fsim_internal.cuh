@@ -242,6 +242,9 @@ struct fsim_sim {
   bool weight_valid = false;
   bool deleted_outside = false;
 
+  // PCG iterations as a CUDA graph with a conditional WHILE node
+  bool use_graphs = true;
+
   // profiling
   bool profiling = false;
   std::vector<fsim::KernelStat> kstats;

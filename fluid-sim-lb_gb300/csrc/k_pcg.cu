@@ -19,9 +19,9 @@
 //           iteration and sets the stop flag.
 // HBM bytes per unknown per iteration: spmv reads r, p_{j-1}, flags and
 // writes p_j (13 B); update reads p_j, x, r, flags and writes x, r (21 B).
-// Each warp owns one leaf: a lane holds two z-columns of 8 cells in
-// registers, neighbours come from warp shuffles and only the six leaf faces
-// are read from the neighbour leaves.  Kernels launched after the stop flag is set return at
+// Each warp owns half a leaf: a lane holds one z-column of 8 cells in
+// registers, neighbours come from warp shuffles and only the faces of the
+// half leaf are read from memory.  Kernels launched after the stop flag is set return at
 // once, so the host polls the flag only between chunks of iterations.
 //
 // Precision modes: FP32 (reference: fp32 vectors, fp32 dots), MIXED (fp32
@@ -37,10 +37,15 @@ namespace fsim {
 
 namespace {
 
-constexpr int kThreads = 256;  // 8 warps; the hot kernels give each warp one leaf
+constexpr int kThreads = 256;     // setup / refinement kernels: one CTA per leaf pass
+constexpr int kHotThreads = 128;  // spmv / update: 4 warps, one half leaf per warp
+// Min resident CTAs per SM requested from ptxas for the hot kernels: 6
+// (80 registers, no spills) for fp32 vectors, 2 for fp64.
 #ifndef FSIM_PCG_MINB
-#define FSIM_PCG_MINB 1  // min resident CTAs per SM requested from ptxas
+#define FSIM_PCG_MINB 6
 #endif
+template <typename T>
+constexpr int hot_minb() { return sizeof(T) == 4 ? FSIM_PCG_MINB : 2; }
 
 // Jacobi: T(1.0/diag) (diag 0 gives inf, as 1.0/0 does in the reference)
 __constant__ float c_invf[8] = {__builtin_inff(), 1.0f, 0.5f, float(1.0 / 3.0),
@@ -99,9 +104,9 @@ struct Dot<2> {
 
 // Block-level sum of NV values.  DM 0 sums in fp32, otherwise fp64.
 // Result valid in thread 0.
-template <int DM, int NV>
+template <int DM, int NV, int NT = kThreads>
 __device__ void block_sum(double (&v)[NV]) {
-  __shared__ double sh[NV][kThreads / 32];
+  __shared__ double sh[NV][NT / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
@@ -124,11 +129,11 @@ __device__ void block_sum(double (&v)[NV]) {
     for (int k = 0; k < NV; ++k) {
       if (DM == 0) {
         float x = 0.f;
-        for (int i = 0; i < kThreads / 32; ++i) x = __fadd_rn(x, float(sh[k][i]));
+        for (int i = 0; i < NT / 32; ++i) x = __fadd_rn(x, float(sh[k][i]));
         v[k] = double(x);
       } else {
         double x = 0.0;
-        for (int i = 0; i < kThreads / 32; ++i) x += sh[k][i];
+        for (int i = 0; i < NT / 32; ++i) x += sh[k][i];
         v[k] = x;
       }
     }
@@ -139,11 +144,11 @@ __device__ void block_sum(double (&v)[NV]) {
 // Single-pass grid reduction: every block deposits its NV partials; the last
 // block to arrive sums them in a fixed order (deterministic) and returns
 // true in all of its threads with the totals in tot (thread 0).
-template <int DM, int NV>
+template <int DM, int NV, int NT = kThreads>
 __device__ bool grid_sum(double (&v)[NV], double* part, int maxb, unsigned int* counter,
                          double (&tot)[NV]) {
   __shared__ bool last;
-  block_sum<DM, NV>(v);
+  block_sum<DM, NV, NT>(v);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) part[k * maxb + blockIdx.x] = v[k];
@@ -154,21 +159,41 @@ __device__ bool grid_sum(double (&v)[NV], double* part, int maxb, unsigned int* 
   __syncthreads();
   if (!last) return false;
   __threadfence();
+  // all partials are read in parallel (8 independent loads in flight per
+  // thread), then summed in a fixed order: deterministic
   double acc[NV];
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
+    const double* pk = part + k * maxb;
     if (DM == 0) {
       float x = 0.f;
-      for (int i = threadIdx.x; i < int(gridDim.x); i += kThreads)
-        x = __fadd_rn(x, float(__ldcg(&part[k * maxb + i])));
+      for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += NT * 8) {
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u * NT;
+          t[u] = i < int(gridDim.x) ? float(__ldcg(pk + i)) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x = __fadd_rn(x, t[u]);
+      }
       acc[k] = double(x);
     } else {
       double x = 0.0;
-      for (int i = threadIdx.x; i < int(gridDim.x); i += kThreads) x += __ldcg(&part[k * maxb + i]);
+      for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += NT * 8) {
+        double t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u * NT;
+          t[u] = i < int(gridDim.x) ? __ldcg(pk + i) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x += t[u];
+      }
       acc[k] = x;
     }
   }
-  block_sum<DM, NV>(acc);
+  block_sum<DM, NV, NT>(acc);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) tot[k] = acc[k];
@@ -194,6 +219,7 @@ struct PcgArgs {
   PcgScalars* sc;
   double* part;
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
+  cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
 };
 
 __device__ __forceinline__ bool converged(const PcgScalars* sc, double rr) {
@@ -275,12 +301,12 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
 }
 
 // ---- column-blocked leaf access -------------------------------------------
-// One warp owns one 8^3 leaf.  Lane L owns the two z-columns (cx, cy) and
-// (cx+4, cy) with cx = L>>3, cy = L&7; a column is 8 contiguous cells
-// (offset x*64 + y*8, 32 B of floats), so the z-neighbours are registers,
-// the y-neighbours are lanes L-1 / L+1 and the x-neighbours lanes L-8 / L+8
-// (or L-24 / L+24 between the two column sets) -- all warp shuffles.  Only
-// the six leaf faces come from the neighbour leaves.  No shared memory and
+// One warp owns half of an 8^3 leaf (x in [0,4) or [4,8)).  Lane L owns the
+// z-column (xb + (L>>3), L&7); a column is 8 contiguous cells (offset
+// x*64 + y*8, 32 B of floats), so the z-neighbours are registers, the
+// y-neighbours are lanes L-1 / L+1 and the x-neighbours lanes L-8 / L+8 --
+// warp shuffles.  Only the faces of the half leaf are read from memory (the
+// other half's boundary plane like a neighbour face).  No shared memory and
 // no CTA barrier in the hot loop.
 template <typename T>
 struct Col {
@@ -373,71 +399,68 @@ __device__ __forceinline__ T ld_pone(const PcgArgs& a, int ns, int vox, const T*
 __device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-// The six face-neighbour slots of leaf s, gathered by lanes 0..5 and
-// broadcast: 0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z.
-__device__ __forceinline__ void face_slots(const int32_t* nb, int lane, int out[6]) {
+// The six face-neighbour slots of a leaf, gathered by lanes 0..5 and
+// broadcast: 0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z.  face_slot_lane loads the
+// lane's entry (issued one half leaf ahead); face_slots broadcasts them.
+__device__ __forceinline__ int face_slot_lane(const int32_t* nbr, int s, int lane) {
   int q = 13;
   if (lane == 0) q = 4; else if (lane == 1) q = 22; else if (lane == 2) q = 10;
   else if (lane == 3) q = 16; else if (lane == 4) q = 12; else if (lane == 5) q = 14;
-  const int mine = (lane < 6) ? __ldg(nb + q) : -1;
+  return (lane < 6) ? __ldg(nbr + int64_t(s) * 27 + q) : -1;
+}
+__device__ __forceinline__ void face_slots(int mine, int out[6]) {
 #pragma unroll
   for (int f = 0; f < 6; ++f) out[f] = __shfl_sync(0xffffffffu, mine, f);
 }
 
-// A p at height z of the lane's two columns P0 (x = cx) and P1 (x = cx+4),
-// summed in the reference's column order (-x,-y,-z, diag, +z,+y,+x).  A lane
-// needs at most one x-face column xh (the -x face when cx == 0, the +x face
-// when cx == 3) and one y-face pair yh0/yh1 (the -y face when cy == 0, the
-// +y face when cy == 7); zm*/zp* are the -z / +z face cells.
+// A p at height z of the lane's column P (x = cx), summed in the
+// reference's column order (-x,-y,-z, diag, +z,+y,+x).  xm/xp: the lane's
+// x-1 / x+1 columns where they are not a neighbour lane (lx == 0 / lx == 3);
+// yh: the y face column (cy == 0: y-1, cy == 7: y+1); zm/zp: z faces.
 template <typename T>
-__device__ __forceinline__ void stencil_z(int z, const Col<T>& P0, const Col<T>& P1, uint8_t g0,
-                                          uint8_t g1, const Col<T>& xh, const Col<T>& yh0,
-                                          const Col<T>& yh1, T zm0, T zp0, T zm1, T zp1,
-                                          int lane, T& a0, T& a1) {
-  const int cx = lane >> 3, cy = lane & 7;
-  const T s_xp0 = (cx == 0) ? P1.v[z] : P0.v[z];
-  const T s_xm1 = (cx == 3) ? P0.v[z] : P1.v[z];
-  const T a_xm0 = shfl(P0.v[z], (lane - 8) & 31);
-  const T a_xp0 = shfl(s_xp0, cx < 3 ? lane + 8 : lane - 24);
-  const T a_xm1 = shfl(s_xm1, cx > 0 ? lane - 8 : lane + 24);
-  const T a_xp1 = shfl(P1.v[z], (lane + 8) & 31);
-  const T a_ym0 = shfl(P0.v[z], (lane - 1) & 31), a_yp0 = shfl(P0.v[z], (lane + 1) & 31);
-  const T a_ym1 = shfl(P1.v[z], (lane - 1) & 31), a_yp1 = shfl(P1.v[z], (lane + 1) & 31);
-  const T xm_0 = cx == 0 ? xh.v[z] : a_xm0;
-  const T xp_1 = cx == 3 ? xh.v[z] : a_xp1;
-  const T ym_0 = cy == 0 ? yh0.v[z] : a_ym0, yp_0 = cy == 7 ? yh0.v[z] : a_yp0;
-  const T ym_1 = cy == 0 ? yh1.v[z] : a_ym1, yp_1 = cy == 7 ? yh1.v[z] : a_yp1;
-  const T zm_0 = z == 0 ? zm0 : P0.v[(z + 7) & 7], zp_0 = z == 7 ? zp0 : P0.v[(z + 1) & 7];
-  const T zm_1 = z == 0 ? zm1 : P1.v[(z + 7) & 7], zp_1 = z == 7 ? zp1 : P1.v[(z + 1) & 7];
+__device__ __forceinline__ T stencil_z(int z, const Col<T>& P, uint8_t g, const Col<T>& xm,
+                                       const Col<T>& xp, const Col<T>& yh, T zm, T zp, int lane) {
+  const int lx = lane >> 3, cy = lane & 7;
+  const T a_xm = shfl(P.v[z], (lane - 8) & 31), a_xp = shfl(P.v[z], (lane + 8) & 31);
+  const T a_ym = shfl(P.v[z], (lane - 1) & 31), a_yp = shfl(P.v[z], (lane + 1) & 31);
+  if (!(g & 1)) return T(0);
+  const T vxm = lx == 0 ? xm.v[z] : a_xm, vxp = lx == 3 ? xp.v[z] : a_xp;
+  const T vym = cy == 0 ? yh.v[z] : a_ym, vyp = cy == 7 ? yh.v[z] : a_yp;
+  const T vzm = z == 0 ? zm : P.v[(z + 7) & 7], vzp = z == 7 ? zp : P.v[(z + 1) & 7];
   T acc = T(0);
-  if (g0 & 1) {
-    acc = tsub(acc, xm_0);
-    acc = tsub(acc, ym_0);
-    acc = tsub(acc, zm_0);
-    acc = tadd(acc, tmul(T(flag_diag(g0)), P0.v[z]));
-    acc = tsub(acc, zp_0);
-    acc = tsub(acc, yp_0);
-    acc = tsub(acc, a_xp0);
-  }
-  a0 = acc;
-  acc = T(0);
-  if (g1 & 1) {
-    acc = tsub(acc, a_xm1);
-    acc = tsub(acc, ym_1);
-    acc = tsub(acc, zm_1);
-    acc = tadd(acc, tmul(T(flag_diag(g1)), P1.v[z]));
-    acc = tsub(acc, zp_1);
-    acc = tsub(acc, yp_1);
-    acc = tsub(acc, xp_1);
-  }
-  a1 = acc;
+  acc = tsub(acc, vxm);
+  acc = tsub(acc, vym);
+  acc = tsub(acc, vzm);
+  acc = tadd(acc, tmul(T(flag_diag(g)), P.v[z]));
+  acc = tsub(acc, vzp);
+  acc = tsub(acc, vyp);
+  acc = tsub(acc, vxp);
+  return acc;
 }
 
-// p_j = z_j + beta_{j-1} p_{j-1} for the leaf and its face halo (z = r/diag
+// Work split of the hot kernels: one warp per half leaf (x in [0,4) or
+// [4,8)); lane -> column (cx = xb + (lane>>3), cy = lane&7).  The other
+// half's boundary plane is read like a face halo.
+struct HalfLeaf {
+  int s, xb, cx, cy, lx, c;
+};
+__device__ __forceinline__ HalfLeaf half_leaf(int hw, int lane) {
+  HalfLeaf h;
+  h.s = hw >> 1;
+  h.xb = (hw & 1) * 4;
+  h.lx = lane >> 3;
+  h.cx = h.xb + h.lx;
+  h.cy = lane & 7;
+  h.c = (h.cx << 6) | (h.cy << 3);
+  return h;
+}
+
+// p_j = z_j + beta_{j-1} p_{j-1} on the half leaf and its halo (z = r/diag
 // recomputed, never stored), then p_j.(A p_j); the last CTA forms alpha_j.
 // Only p_j is written: the update kernel recomputes A p_j from it.
 template <typename T, int DM>
-__global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_spmv(const __grid_constant__ PcgArgs a) {
+__global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
+    k_pcg_spmv(const __grid_constant__ PcgArgs a) {
   const PcgScalars* sc = a.sc;
   if (sc->done) return;
   const int it = sc->iter;
@@ -447,56 +470,50 @@ __global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_spmv(const __gr
   const T* pold = static_cast<const T*>((it & 1) ? a.p0 : a.p1);
   T* pnew = static_cast<T*>((it & 1) ? a.p1 : a.p0);
   const int lane = threadIdx.x & 31;
-  const int cx = lane >> 3, cy = lane & 7;
-  const int c0 = (cx << 6) | (cy << 3), c1 = ((cx + 4) << 6) | (cy << 3);
-  const int wpb = kThreads / 32;
+  const int wpb = kHotThreads / 32;
   Dot<DM> dp;
-  for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < a.n_pleaf; s += gridDim.x * wpb) {
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  for (; hw < nhw; hw += hstride) {
+    const int nbl_next = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+    const HalfLeaf h = half_leaf(hw, lane);
+    const int64_t base = int64_t(h.s) * 512;
+    // own column first (independent of the neighbour table)
+    const uint2 f = ldflags(a.flags, base + h.c);
+    Col<T> rc, pc;
+    ldcol(r, base + h.c, rc);
+    if (!first) ldcol(pold, base + h.c, pc);
     int fs[6];
-    face_slots(a.nbr + int64_t(s) * 27, lane, fs);
-    const int64_t base = int64_t(s) * 512;
-    const uint2 f0 = ldflags(a.flags, base + c0), f1 = ldflags(a.flags, base + c1);
-    Col<T> r0, r1, q0, q1;
-    ldcol(r, base + c0, r0);
-    ldcol(r, base + c1, r1);
-    if (!first) {
-      ldcol(pold, base + c0, q0);
-      ldcol(pold, base + c1, q1);
-    }
-    // face halos (p_new computed from the neighbour's r, p_old, flags)
-    Col<T> xh, yh0, yh1;
-    if (cx == 0 || cx == 3)
-      pnew_column(a, cx == 0 ? fs[0] : fs[1], ((cx == 0 ? 7 : 0) << 6) | (cy << 3), beta, first,
-                  r, pold, xh);
-    if (cy == 0 || cy == 7) {
-      const int ns = cy == 0 ? fs[2] : fs[3], yy = (cy == 0 ? 7 : 0) << 3;
-      pnew_column(a, ns, (cx << 6) | yy, beta, first, r, pold, yh0);
-      pnew_column(a, ns, ((cx + 4) << 6) | yy, beta, first, r, pold, yh1);
-    }
-    const T zm0 = pnew_one(a, fs[4], c0 | 7, beta, first, r, pold);
-    const T zm1 = pnew_one(a, fs[4], c1 | 7, beta, first, r, pold);
-    const T zp0 = pnew_one(a, fs[5], c0, beta, first, r, pold);
-    const T zp1 = pnew_one(a, fs[5], c1, beta, first, r, pold);
-    Col<T> P0, P1;
+    face_slots(nbl, fs);
+    nbl = nbl_next;
+    Col<T> xm, xp, yh;
+    if (h.lx == 0)  // x-1: the -x leaf (xb 0) or this leaf's x=3 plane (xb 4)
+      pnew_column(a, h.xb == 0 ? fs[0] : h.s, ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3), beta,
+                  first, r, pold, xm);
+    if (h.lx == 3)  // x+1: this leaf's x=4 plane (xb 0) or the +x leaf (xb 4)
+      pnew_column(a, h.xb == 0 ? h.s : fs[1], ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3), beta,
+                  first, r, pold, xp);
+    if (h.cy == 0 || h.cy == 7)
+      pnew_column(a, h.cy == 0 ? fs[2] : fs[3], (h.cx << 6) | ((h.cy == 0 ? 7 : 0) << 3), beta,
+                  first, r, pold, yh);
+    const T zm = pnew_one(a, fs[4], h.c | 7, beta, first, r, pold);
+    const T zp = pnew_one(a, fs[5], h.c, beta, first, r, pold);
+    Col<T> P;
+#pragma unroll
+    for (int z = 0; z < 8; ++z)
+      P.v[z] = pnew_cell<T>(fbyte(f, z), rc.v[z], first ? T(0) : pc.v[z], beta, first);
+    stcol(pnew, base + h.c, P);
 #pragma unroll
     for (int z = 0; z < 8; ++z) {
-      P0.v[z] = pnew_cell<T>(fbyte(f0, z), r0.v[z], first ? T(0) : q0.v[z], beta, first);
-      P1.v[z] = pnew_cell<T>(fbyte(f1, z), r1.v[z], first ? T(0) : q1.v[z], beta, first);
-    }
-    stcol(pnew, base + c0, P0);
-    stcol(pnew, base + c1, P1);
-#pragma unroll
-    for (int z = 0; z < 8; ++z) {
-      const uint8_t g0 = fbyte(f0, z), g1 = fbyte(f1, z);
-      T a0, a1;
-      stencil_z<T>(z, P0, P1, g0, g1, xh, yh0, yh1, zm0, zp0, zm1, zp1, lane, a0, a1);
-      if (g0 & 1) dp.add(P0.v[z], a0);
-      if (g1 & 1) dp.add(P1.v[z], a1);
+      const uint8_t g = fbyte(f, z);
+      const T ap = stencil_z<T>(z, P, g, xm, xp, yh, zm, zp, lane);
+      if (g & 1) dp.add(P.v[z], ap);
     }
   }
   double v[1] = {dp.value()};
   double tot[1];
-  if (grid_sum<DM, 1>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
+  if (grid_sum<DM, 1, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
     PcgScalars* s = a.sc;
     s->pAp = round_t(s, tot[0]);
     double alpha = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->pAp))) : s->rz / s->pAp;
@@ -508,12 +525,18 @@ __global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_spmv(const __gr
   }
 }
 
-// A p_j recomputed from p_j (leaf + face halo); x += alpha p;
+// A p_j recomputed from p_j (half leaf + halo); x += alpha p;
 // r -= alpha Ap; r.r and r.z; the last CTA forms beta and the stop test.
 template <typename T, int DM>
-__global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_update(const __grid_constant__ PcgArgs a) {
+__global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
+    k_pcg_update(const __grid_constant__ PcgArgs a) {
   const PcgScalars* sc = a.sc;
-  if (sc->done) return;
+  if (sc->done) {
+    // stop flag already set (converged at setup, or breakdown in spmv):
+    // end the graph's WHILE loop
+    if (a.cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
+    return;
+  }
   const int it = sc->iter;
   const T alpha = T(sc->alpha);
   const T nalpha = -alpha;
@@ -521,58 +544,49 @@ __global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_update(const __
   T* x = static_cast<T*>(a.x);
   T* r = static_cast<T*>(a.r);
   const int lane = threadIdx.x & 31;
-  const int cx = lane >> 3, cy = lane & 7;
-  const int c0 = (cx << 6) | (cy << 3), c1 = ((cx + 4) << 6) | (cy << 3);
-  const int wpb = kThreads / 32;
+  const int wpb = kHotThreads / 32;
   Dot<DM> drr, drz;
-  for (int s = blockIdx.x * wpb + (threadIdx.x >> 5); s < a.n_pleaf; s += gridDim.x * wpb) {
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  for (; hw < nhw; hw += hstride) {
+    const int nbl_next = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+    const HalfLeaf h = half_leaf(hw, lane);
+    const int64_t base = int64_t(h.s) * 512;
+    const uint2 f = ldflags(a.flags, base + h.c);
+    Col<T> P;
+    ldcol(p, base + h.c, P);
     int fs[6];
-    face_slots(a.nbr + int64_t(s) * 27, lane, fs);
-    const int64_t base = int64_t(s) * 512;
-    const uint2 f0 = ldflags(a.flags, base + c0), f1 = ldflags(a.flags, base + c1);
-    Col<T> P0, P1, x0, x1, r0, r1;
-    ldcol(p, base + c0, P0);
-    ldcol(p, base + c1, P1);
-    Col<T> xh, yh0, yh1;
-    if (cx == 0 || cx == 3)
-      ld_pcol(a, cx == 0 ? fs[0] : fs[1], ((cx == 0 ? 7 : 0) << 6) | (cy << 3), p, xh);
-    if (cy == 0 || cy == 7) {
-      const int ns = cy == 0 ? fs[2] : fs[3], yy = (cy == 0 ? 7 : 0) << 3;
-      ld_pcol(a, ns, (cx << 6) | yy, p, yh0);
-      ld_pcol(a, ns, ((cx + 4) << 6) | yy, p, yh1);
-    }
-    const T zm0 = ld_pone(a, fs[4], c0 | 7, p), zm1 = ld_pone(a, fs[4], c1 | 7, p);
-    const T zp0 = ld_pone(a, fs[5], c0, p), zp1 = ld_pone(a, fs[5], c1, p);
-    ldcol(x, base + c0, x0);
-    ldcol(x, base + c1, x1);
-    ldcol(r, base + c0, r0);
-    ldcol(r, base + c1, r1);
+    face_slots(nbl, fs);
+    nbl = nbl_next;
+    Col<T> xm, xp, yh;
+    if (h.lx == 0)
+      ld_pcol(a, h.xb == 0 ? fs[0] : h.s, ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3), p, xm);
+    if (h.lx == 3)
+      ld_pcol(a, h.xb == 0 ? h.s : fs[1], ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3), p, xp);
+    if (h.cy == 0 || h.cy == 7)
+      ld_pcol(a, h.cy == 0 ? fs[2] : fs[3], (h.cx << 6) | ((h.cy == 0 ? 7 : 0) << 3), p, yh);
+    const T zm = ld_pone(a, fs[4], h.c | 7, p), zp = ld_pone(a, fs[5], h.c, p);
+    Col<T> xc, rc;
+    ldcol(x, base + h.c, xc);
+    ldcol(r, base + h.c, rc);
 #pragma unroll
     for (int z = 0; z < 8; ++z) {
-      const uint8_t g0 = fbyte(f0, z), g1 = fbyte(f1, z);
-      T a0, a1;
-      stencil_z<T>(z, P0, P1, g0, g1, xh, yh0, yh1, zm0, zp0, zm1, zp1, lane, a0, a1);
-      x0.v[z] = tadd(tmul(alpha, P0.v[z]), x0.v[z]);
-      x1.v[z] = tadd(tmul(alpha, P1.v[z]), x1.v[z]);
-      r0.v[z] = tadd(tmul(nalpha, a0), r0.v[z]);
-      r1.v[z] = tadd(tmul(nalpha, a1), r1.v[z]);
-      if (g0 & 1) {
-        drr.add(r0.v[z], r0.v[z]);
-        drz.add(r0.v[z], tmul(inv_diag<T>(g0), r0.v[z]));
-      }
-      if (g1 & 1) {
-        drr.add(r1.v[z], r1.v[z]);
-        drz.add(r1.v[z], tmul(inv_diag<T>(g1), r1.v[z]));
+      const uint8_t g = fbyte(f, z);
+      const T ap = stencil_z<T>(z, P, g, xm, xp, yh, zm, zp, lane);
+      xc.v[z] = tadd(tmul(alpha, P.v[z]), xc.v[z]);
+      rc.v[z] = tadd(tmul(nalpha, ap), rc.v[z]);
+      if (g & 1) {
+        drr.add(rc.v[z], rc.v[z]);
+        drz.add(rc.v[z], tmul(inv_diag<T>(g), rc.v[z]));
       }
     }
-    stcol(x, base + c0, x0);
-    stcol(x, base + c1, x1);
-    stcol(r, base + c0, r0);
-    stcol(r, base + c1, r1);
+    stcol(x, base + h.c, xc);
+    stcol(r, base + h.c, rc);
   }
   double v[2] = {drr.value(), drz.value()};
   double tot[2];
-  if (grid_sum<DM, 2>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
+  if (grid_sum<DM, 2, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
     PcgScalars* s = a.sc;
     s->rr = round_t(s, tot[0]);
     s->rz_old = s->rz;
@@ -586,6 +600,7 @@ __global__ void __launch_bounds__(kThreads, FSIM_PCG_MINB) k_pcg_update(const __
     } else {
       s->done = (s->iter >= s->max_iter) || converged(s, s->rr);
     }
+    if (a.cond) cudaGraphSetConditional(a.cond, s->done ? 0u : 1u);
   }
 }
 
@@ -639,13 +654,85 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
     pres[o] = float(x[o]);
 }
 
+// Builds and launches graph = WHILE(cond){ spmv; update } on the handle's
+// stream.  Returns FSIM_OK, or FSIM_ERR_CUDA when the graph API refuses
+// (the caller then polls from the host).  Kernel launches inside the graph
+// are counted by the caller from the iteration count the solve reports.
+template <typename T, int DM>
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid) {
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  if (e == cudaSuccess) {
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    a.cond = h;
+    cudaKernelNodeParams kp;
+    memset(&kp, 0, sizeof(kp));
+    void* args[] = {&a};
+    kp.gridDim = dim3(unsigned(wgrid));
+    kp.blockDim = dim3(unsigned(kHotThreads));
+    kp.kernelParams = args;
+    cudaGraphNode_t n1 = nullptr, n2 = nullptr;
+    kp.func = reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+    e = cudaGraphAddKernelNode(&n1, body, nullptr, 0, &kp);
+    if (e == cudaSuccess) {
+      kp.func = reinterpret_cast<void*>(k_pcg_update<T, DM>);
+      e = cudaGraphAddKernelNode(&n2, body, &n1, 1, &kp);
+    }
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+  if (e == cudaSuccess) e = cudaGraphLaunch(ge, s->stream);
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // clear the (non-sticky) error of the refused call
+    return FSIM_ERR_CUDA;
+  }
+  return FSIM_OK;
+}
+
+// One inner solve: setup, then the iterations.  The iterations run as a CUDA
+// graph whose conditional WHILE node repeats {spmv, update}; the update
+// kernel's last CTA clears the condition when the stop flag is set, so the
+// whole loop runs without a host round trip.  The loop is bounded by the
+// solve's max_iterations (the stop flag is set at that count).  If graph
+// construction is not available the host launches chunks of iterations and
+// polls the stop flag between them (kernels launched after it is set return
+// at once).
 template <typename T, int DM>
 int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const char* nm_spmv,
               const char* nm_upd) {
+  a.cond = 0;
   FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
-  // hot kernels: one warp per leaf, kThreads/32 leaves per CTA
-  const int wgrid = std::max(1, std::min((a.n_pleaf + kThreads / 32 - 1) / (kThreads / 32),
-                                         s->max_blocks));
+  const int wpb = kHotThreads / 32;
+  int occ_a = 1, occ_b = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_pcg_spmv<T, DM>, kHotThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_pcg_update<T, DM>, kHotThreads, 0);
+  const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
+  const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
+                                          s->max_blocks}));
+  if (s->use_graphs && !s->profiling) {
+    int rc = run_graph_loop<T, DM>(s, a, wgrid);
+    if (rc == FSIM_OK) {
+      FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                 s->stream));
+      FSIM_CK(s, cudaStreamSynchronize(s->stream));
+      // each WHILE pass runs both kernels; one pass follows a stop at setup
+      s->launches += 2 * int64_t(std::max(s->h_sc->iter + (s->h_sc->status ? 1 : 0), 1));
+      return FSIM_OK;
+    }
+    s->use_graphs = false;  // fall back for the rest of this handle's life
+  }
+  a.cond = 0;
   int chunk = 8;
   for (;;) {
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
@@ -653,8 +740,8 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     FSIM_CK(s, cudaStreamSynchronize(s->stream));
     if (s->h_sc->done) break;
     for (int c = 0; c < chunk; ++c) {
-      FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kThreads, 0, a);
-      FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kThreads, 0, a);
+      FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kHotThreads, 0, a);
+      FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kHotThreads, 0, a);
     }
     if (chunk < 64) chunk *= 2;
   }
