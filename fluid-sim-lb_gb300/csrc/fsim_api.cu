@@ -192,7 +192,7 @@ int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf) {
     dfree(s->d_cell_range); dfree(s->d_leaf_range);
     dfree(s->div); dfree(s->pres); dfree(s->r); dfree(s->p[0]); dfree(s->p[1]); dfree(s->Ap);
     dfree(s->flags); dfree(s->x64); dfree(s->r64); dfree(s->p64[0]); dfree(s->p64[1]);
-    dfree(s->Ap64); dfree(s->b64);
+    dfree(s->Ap64); dfree(s->b64); dfree(s->zface); dfree(s->zface64); dfree(s->zflags);
     const size_t n = size_t(cap) * 512;
     if ((rc = dmalloc(s, &s->d_cell_range, n))) return rc;
     if ((rc = dmalloc(s, &s->d_leaf_range, size_t(cap)))) return rc;
@@ -201,8 +201,9 @@ int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf) {
     if ((rc = dmalloc(s, &s->r, n))) return rc;
     if ((rc = dmalloc(s, &s->p[0], n))) return rc;
     if ((rc = dmalloc(s, &s->p[1], n))) return rc;
-    if ((rc = dmalloc(s, &s->Ap, n))) return rc;
     if ((rc = dmalloc(s, &s->flags, n))) return rc;
+    if ((rc = dmalloc(s, &s->zface, size_t(cap) * 384))) return rc;
+    if ((rc = dmalloc(s, &s->zflags, size_t(cap) * 128))) return rc;
     s->cap_pleaf = cap;
   }
   return FSIM_OK;
@@ -285,7 +286,8 @@ int fsim_destroy(fsim_t* s) {
   dfree(s->d_cell_range); dfree(s->d_leaf_range);
   dfree(s->vel); dfree(s->vold); dfree(s->weight); dfree(s->vel_on); dfree(s->vold_on);
   dfree(s->marker); dfree(s->div); dfree(s->pres); dfree(s->r); dfree(s->p[0]); dfree(s->p[1]);
-  dfree(s->Ap); dfree(s->flags); dfree(s->x64); dfree(s->r64); dfree(s->p64[0]);
+  dfree(s->Ap); dfree(s->flags); dfree(s->zface); dfree(s->zface64); dfree(s->zflags);
+  dfree(s->x64); dfree(s->r64); dfree(s->p64[0]);
   dfree(s->p64[1]); dfree(s->Ap64); dfree(s->b64); dfree(s->d_sc); dfree(s->d_part);
   dfree(s->d_partf); dfree(s->d_cnt);
   if (s->dense_tmp.p) cudaFree(s->dense_tmp.p);

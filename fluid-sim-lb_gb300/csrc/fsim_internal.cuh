@@ -215,6 +215,13 @@ struct fsim_sim {
   float* p[2] = {nullptr, nullptr};
   float* Ap = nullptr;
   uint8_t* flags = nullptr;
+  // z-face planes per particle leaf (z=0 and z=7, 64 cells each, x*8+y):
+  // [r | p_a | p_b] planes and the flags planes, so that a leaf's -z / +z
+  // neighbour cells are read contiguously (in the cell layout x*64+y*8+z a
+  // z face is 64 scattered cells)
+  float* zface = nullptr;     // pleaf * 384
+  double* zface64 = nullptr;  // pleaf * 384 (FP64 mode)
+  uint8_t* zflags = nullptr;  // pleaf * 128
   double* x64 = nullptr;  // mixed / fp64 solution
   double* r64 = nullptr;  // fp64 mode vectors
   double* p64[2] = {nullptr, nullptr};

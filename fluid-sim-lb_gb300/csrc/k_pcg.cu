@@ -213,7 +213,8 @@ struct PcgArgs {
   void* r;
   void* p0;
   void* p1;
-  void* Ap;
+  void* zf;         // z-face planes [leaf][r | p_a | p_b][plane][x*8+y]
+  uint8_t* zff;     // flags z-face planes [leaf][plane][x*8+y]
   double* x64;      // MIXED outer solution
   float* dinner;    // MIXED inner solution (the fp32 x of the inner solve)
   PcgScalars* sc;
@@ -274,6 +275,11 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
       } else {
         rv = r[o];
       }
+      if (cz == 0 || cz == 7) {
+        const int fi = (cz == 7 ? 64 : 0) + cx * 8 + cy;
+        a.zff[int64_t(s) * 128 + fi] = f;
+        static_cast<T*>(a.zf)[int64_t(s) * 384 + fi] = rv;
+      }
       const T z = tmul(inv_diag<T>(f), rv);
       drr.add(rv, rv);
       drz.add(rv, z);
@@ -313,16 +319,31 @@ struct Col {
   T v[8];
 };
 
+// Column loads: a lane reads its 32 B column as two 16 B vectors.  With the
+// default (L1-allocating) load the second vector hits the line the first
+// brought in; FSIM_PCG_LDCG=1 selects L2-only loads instead.
+#ifndef FSIM_PCG_LDCG
+#define FSIM_PCG_LDCG 0
+#endif
+template <typename V>
+__device__ __forceinline__ V ldv(const V* p) {
+#if FSIM_PCG_LDCG
+  return __ldcg(p);
+#else
+  return *p;
+#endif
+}
+
 __device__ __forceinline__ void ldcol(const float* __restrict__ p, int64_t o, Col<float>& c) {
-  const float4 a = __ldcg(reinterpret_cast<const float4*>(p + o));
-  const float4 b = __ldcg(reinterpret_cast<const float4*>(p + o + 4));
+  const float4 a = ldv(reinterpret_cast<const float4*>(p + o));
+  const float4 b = ldv(reinterpret_cast<const float4*>(p + o + 4));
   c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
   c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
 }
 __device__ __forceinline__ void ldcol(const double* __restrict__ p, int64_t o, Col<double>& c) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const double2 a = __ldcg(reinterpret_cast<const double2*>(p + o + 2 * k));
+    const double2 a = ldv(reinterpret_cast<const double2*>(p + o + 2 * k));
     c.v[2 * k] = a.x;
     c.v[2 * k + 1] = a.y;
   }
@@ -337,64 +358,15 @@ __device__ __forceinline__ void stcol(double* __restrict__ p, int64_t o, const C
     *reinterpret_cast<double2*>(p + o + 2 * k) = make_double2(c.v[2 * k], c.v[2 * k + 1]);
 }
 __device__ __forceinline__ uint2 ldflags(const uint8_t* __restrict__ f, int64_t o) {
-  return __ldcg(reinterpret_cast<const uint2*>(f + o));
+  return ldv(reinterpret_cast<const uint2*>(f + o));
 }
 __device__ __forceinline__ uint8_t fbyte(uint2 f, int z) {
   return uint8_t((z < 4 ? f.x : f.y) >> (8 * (z & 3)));
 }
 
-// p = z + beta p_old with z = r/diag (p = z at the first iteration); 0 off-fluid
-template <typename T>
-__device__ __forceinline__ T pnew_cell(uint8_t f, T r, T po, T beta, bool first) {
-  if (!(f & 1)) return T(0);
-  const T z = tmul(inv_diag<T>(f), r);
-  return first ? z : tadd(z, tmul(beta, po));
-}
 
-// p_new of a whole neighbour column (spmv: from r, p_old, flags)
-template <typename T>
-__device__ __forceinline__ void pnew_column(const PcgArgs& a, int ns, int vox0, T beta, bool first,
-                                            const T* r, const T* pold, Col<T>& out) {
-  if (ns < 0 || ns >= a.n_pleaf) {
-#pragma unroll
-    for (int z = 0; z < 8; ++z) out.v[z] = T(0);
-    return;
-  }
-  const int64_t o = int64_t(ns) * 512 + vox0;
-  const uint2 f = ldflags(a.flags, o);
-  Col<T> rc, pc;
-  ldcol(r, o, rc);
-  if (!first) ldcol(pold, o, pc);
-#pragma unroll
-  for (int z = 0; z < 8; ++z) out.v[z] = pnew_cell<T>(fbyte(f, z), rc.v[z], first ? T(0) : pc.v[z],
-                                                     beta, first);
-}
 
-// p_new of one neighbour cell (z faces)
-template <typename T>
-__device__ __forceinline__ T pnew_one(const PcgArgs& a, int ns, int vox, T beta, bool first,
-                                      const T* r, const T* pold) {
-  if (ns < 0 || ns >= a.n_pleaf) return T(0);
-  const int64_t o = int64_t(ns) * 512 + vox;
-  const uint8_t f = __ldcg(a.flags + o);
-  return pnew_cell<T>(f, __ldcg(r + o), first ? T(0) : __ldcg(pold + o), beta, first);
-}
 
-template <typename T>
-__device__ __forceinline__ void ld_pcol(const PcgArgs& a, int ns, int vox0, const T* p, Col<T>& out) {
-  if (ns < 0 || ns >= a.n_pleaf) {
-#pragma unroll
-    for (int z = 0; z < 8; ++z) out.v[z] = T(0);
-    return;
-  }
-  ldcol(p, int64_t(ns) * 512 + vox0, out);
-}
-
-template <typename T>
-__device__ __forceinline__ T ld_pone(const PcgArgs& a, int ns, int vox, const T* p) {
-  if (ns < 0 || ns >= a.n_pleaf) return T(0);
-  return __ldcg(p + int64_t(ns) * 512 + vox);
-}
 
 __device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
@@ -413,46 +385,131 @@ __device__ __forceinline__ void face_slots(int mine, int out[6]) {
   for (int f = 0; f < 6; ++f) out[f] = __shfl_sync(0xffffffffu, mine, f);
 }
 
-// A p at height z of the lane's column P (x = cx), summed in the
-// reference's column order (-x,-y,-z, diag, +z,+y,+x).  xm/xp: the lane's
-// x-1 / x+1 columns where they are not a neighbour lane (lx == 0 / lx == 3);
-// yh: the y face column (cy == 0: y-1, cy == 7: y+1); zm/zp: z faces.
-template <typename T>
-__device__ __forceinline__ T stencil_z(int z, const Col<T>& P, uint8_t g, const Col<T>& xm,
-                                       const Col<T>& xp, const Col<T>& yh, T zm, T zp, int lane) {
-  const int lx = lane >> 3, cy = lane & 7;
-  const T a_xm = shfl(P.v[z], (lane - 8) & 31), a_xp = shfl(P.v[z], (lane + 8) & 31);
-  const T a_ym = shfl(P.v[z], (lane - 1) & 31), a_yp = shfl(P.v[z], (lane + 1) & 31);
-  if (!(g & 1)) return T(0);
-  const T vxm = lx == 0 ? xm.v[z] : a_xm, vxp = lx == 3 ? xp.v[z] : a_xp;
-  const T vym = cy == 0 ? yh.v[z] : a_ym, vyp = cy == 7 ? yh.v[z] : a_yp;
-  const T vzm = z == 0 ? zm : P.v[(z + 7) & 7], vzp = z == 7 ? zp : P.v[(z + 1) & 7];
-  T acc = T(0);
-  acc = tsub(acc, vxm);
-  acc = tsub(acc, vym);
-  acc = tsub(acc, vzm);
-  acc = tadd(acc, tmul(T(flag_diag(g)), P.v[z]));
-  acc = tsub(acc, vzp);
-  acc = tsub(acc, vyp);
-  acc = tsub(acc, vxp);
-  return acc;
-}
-
-// Work split of the hot kernels: one warp per half leaf (x in [0,4) or
-// [4,8)); lane -> column (cx = xb + (lane>>3), cy = lane&7).  The other
-// half's boundary plane is read like a face halo.
+// Work split of the hot kernels: one warp per half leaf (x in [xb, xb+4),
+// xb = 0 or 4).  Lane (lx = lane>>3, cy = lane&7) owns the interior column
+// (xb+lx, cy) and loads one face column of the half leaf's halo:
+//   lx == 0: plane x = xb-1, column cy  (-x leaf, or this leaf's x=3 plane)
+//   lx == 3: plane x = xb+4, column cy  (this leaf's x=4 plane, or +x leaf)
+//   lx == 1: cy < 4: -y leaf column (xb+cy, 7); cy >= 4: +y leaf (xb+cy-4, 0)
+//   lx == 2: none
+// plus its own column's -z / +z face cells.  Columns are staged in a
+// per-warp shared tile [x: xb-1..xb+4][y: -1..8][z: 0..7]; each lane then
+// reads its four x/y neighbour columns with 16 B shared loads.
 struct HalfLeaf {
-  int s, xb, cx, cy, lx, c;
+  int s, xb, lx, cy, c;
+  int hslot, hvox;  // halo column (leaf slot, first voxel); hslot -1: none
+  int tx, ty;       // halo column position in the tile
 };
-__device__ __forceinline__ HalfLeaf half_leaf(int hw, int lane) {
+__device__ __forceinline__ HalfLeaf half_leaf(int hw, int lane, const int fs[6]) {
   HalfLeaf h;
   h.s = hw >> 1;
   h.xb = (hw & 1) * 4;
   h.lx = lane >> 3;
-  h.cx = h.xb + h.lx;
   h.cy = lane & 7;
-  h.c = (h.cx << 6) | (h.cy << 3);
+  h.c = ((h.xb + h.lx) << 6) | (h.cy << 3);
+  h.hslot = -1;
+  h.hvox = 0;
+  h.tx = 0;
+  h.ty = 0;
+  if (h.lx == 0) {
+    h.hslot = h.xb == 0 ? fs[0] : h.s;
+    h.hvox = ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3);
+    h.tx = 0;
+    h.ty = h.cy + 1;
+  } else if (h.lx == 3) {
+    h.hslot = h.xb == 0 ? h.s : fs[1];
+    h.hvox = ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3);
+    h.tx = 5;
+    h.ty = h.cy + 1;
+  } else if (h.lx == 1) {
+    const bool lo = h.cy < 4;
+    const int hx = h.cy & 3;
+    h.hslot = lo ? fs[2] : fs[3];
+    h.hvox = ((h.xb + hx) << 6) | ((lo ? 7 : 0) << 3);
+    h.tx = hx + 1;
+    h.ty = lo ? 0 : 9;
+  }
   return h;
+}
+
+// Jacobi inverse diagonal T(1.0/diag) by an exact select chain (pure ALU);
+// diag 0 gives inf as 1.0/0 does; 0 for cells that are not FLUID.
+template <typename T>
+__device__ __forceinline__ T inv_sel(uint8_t f) {
+  const int d = flag_diag(f);
+  T v = T(1.0 / 7.0);
+  v = d == 6 ? T(1.0 / 6.0) : v;
+  v = d == 5 ? T(1.0 / 5.0) : v;
+  v = d == 4 ? T(0.25) : v;
+  v = d == 3 ? T(1.0 / 3.0) : v;
+  v = d == 2 ? T(0.5) : v;
+  v = d == 1 ? T(1.0) : v;
+  v = d == 0 ? T(__builtin_inf()) : v;
+  return (f & 1) ? v : T(0);
+}
+
+template <typename T>
+struct __align__(16) Tile {
+  T c[6][10][8];  // [x - xb + 1][y + 1][z]; 16 B aligned for vector access
+};
+
+__device__ __forceinline__ void st_col_sh(float* p, const Col<float>& c) {
+  reinterpret_cast<float4*>(p)[0] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
+  reinterpret_cast<float4*>(p)[1] = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
+}
+__device__ __forceinline__ void st_col_sh(double* p, const Col<double>& c) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    reinterpret_cast<double2*>(p)[k] = make_double2(c.v[2 * k], c.v[2 * k + 1]);
+}
+__device__ __forceinline__ void ld_col_sh(const float* p, Col<float>& c) {
+  const float4 a = reinterpret_cast<const float4*>(p)[0];
+  const float4 b = reinterpret_cast<const float4*>(p)[1];
+  c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
+  c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
+}
+__device__ __forceinline__ void ld_col_sh(const double* p, Col<double>& c) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double2 a = reinterpret_cast<const double2*>(p)[k];
+    c.v[2 * k] = a.x;
+    c.v[2 * k + 1] = a.y;
+  }
+}
+
+// A p on the lane's column, summed in the reference's column order
+// (-x,-y,-z, diag, +z,+y,+x); 0 off-fluid.  The four x/y neighbour columns
+// come from the tile; zm / zp are the -z / +z face cells.
+template <typename T>
+__device__ __forceinline__ void stencil_col(const Tile<T>& t, int lx, int cy, const Col<T>& P,
+                                            uint2 f, T zm, T zp, Col<T>& out) {
+  Col<T> xm, xp, ym, yp;
+  ld_col_sh(t.c[lx][cy + 1], xm);
+  ld_col_sh(t.c[lx + 2][cy + 1], xp);
+  ld_col_sh(t.c[lx + 1][cy], ym);
+  ld_col_sh(t.c[lx + 1][cy + 2], yp);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) {
+    const uint8_t g = fbyte(f, z);
+    const T vzm = z == 0 ? zm : P.v[(z + 7) & 7], vzp = z == 7 ? zp : P.v[(z + 1) & 7];
+    T acc = T(0);
+    acc = tsub(acc, xm.v[z]);
+    acc = tsub(acc, ym.v[z]);
+    acc = tsub(acc, vzm);
+    acc = tadd(acc, tmul(T(flag_diag(g)), P.v[z]));
+    acc = tsub(acc, vzp);
+    acc = tsub(acc, yp.v[z]);
+    acc = tsub(acc, xp.v[z]);
+    out.v[z] = (g & 1) ? acc : T(0);
+  }
+}
+
+// p = z + beta p_old with z = r/diag (p = z at the first iteration); 0 off-fluid
+template <typename T>
+__device__ __forceinline__ T pnew_of(uint8_t f, T r, T po, T beta, bool first) {
+  const T z = tmul(inv_sel<T>(f), r);
+  const T v = first ? z : tadd(z, tmul(beta, po));
+  return (f & 1) ? v : T(0);
 }
 
 // p_j = z_j + beta_{j-1} p_{j-1} on the half leaf and its halo (z = r/diag
@@ -461,6 +518,7 @@ __device__ __forceinline__ HalfLeaf half_leaf(int hw, int lane) {
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_spmv(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
   const PcgScalars* sc = a.sc;
   if (sc->done) return;
   const int it = sc->iter;
@@ -470,6 +528,7 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   const T* pold = static_cast<const T*>((it & 1) ? a.p0 : a.p1);
   T* pnew = static_cast<T*>((it & 1) ? a.p1 : a.p0);
   const int lane = threadIdx.x & 31;
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
   const int wpb = kHotThreads / 32;
   Dot<DM> dp;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
@@ -477,39 +536,63 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
   for (; hw < nhw; hw += hstride) {
     const int nbl_next = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
-    const HalfLeaf h = half_leaf(hw, lane);
+    int fs[6];
+    face_slots(nbl, fs);
+    nbl = nbl_next;
+    const HalfLeaf h = half_leaf(hw, lane, fs);
     const int64_t base = int64_t(h.s) * 512;
-    // own column first (independent of the neighbour table)
+    // own column
     const uint2 f = ldflags(a.flags, base + h.c);
     Col<T> rc, pc;
     ldcol(r, base + h.c, rc);
     if (!first) ldcol(pold, base + h.c, pc);
-    int fs[6];
-    face_slots(nbl, fs);
-    nbl = nbl_next;
-    Col<T> xm, xp, yh;
-    if (h.lx == 0)  // x-1: the -x leaf (xb 0) or this leaf's x=3 plane (xb 4)
-      pnew_column(a, h.xb == 0 ? fs[0] : h.s, ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3), beta,
-                  first, r, pold, xm);
-    if (h.lx == 3)  // x+1: this leaf's x=4 plane (xb 0) or the +x leaf (xb 4)
-      pnew_column(a, h.xb == 0 ? h.s : fs[1], ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3), beta,
-                  first, r, pold, xp);
-    if (h.cy == 0 || h.cy == 7)
-      pnew_column(a, h.cy == 0 ? fs[2] : fs[3], (h.cx << 6) | ((h.cy == 0 ? 7 : 0) << 3), beta,
-                  first, r, pold, yh);
-    const T zm = pnew_one(a, fs[4], h.c | 7, beta, first, r, pold);
-    const T zp = pnew_one(a, fs[5], h.c, beta, first, r, pold);
-    Col<T> P;
-#pragma unroll
-    for (int z = 0; z < 8; ++z)
-      P.v[z] = pnew_cell<T>(fbyte(f, z), rc.v[z], first ? T(0) : pc.v[z], beta, first);
-    stcol(pnew, base + h.c, P);
+    // halo column
+    const bool hv = h.hslot >= 0 && h.hslot < a.n_pleaf;
+    const int64_t hb = int64_t(hv ? h.hslot : 0) * 512 + h.hvox;
+    uint2 hf = make_uint2(0u, 0u);
+    Col<T> hr, hp;
+    if (hv) {
+      hf = ldflags(a.flags, hb);
+      ldcol(r, hb, hr);
+      if (!first) ldcol(pold, hb, hp);
+    }
+    // z faces of the own column, from the neighbours' published planes:
+    // the -z leaf's z=7 plane and the +z leaf's z=0 plane
+    const int zs0 = fs[4], zs1 = fs[5];
+    const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+    const int fidx = (h.xb + h.lx) * 8 + h.cy;
+    const T* zf = static_cast<const T*>(a.zf);
+    const int qold = 1 + ((it + 1) & 1), qnew = 1 + (it & 1);
+    const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + fidx;
+    const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + fidx;
+    const uint8_t zf0 = zv0 ? ldv(a.zff + int64_t(zs0) * 128 + 64 + fidx) : uint8_t(0);
+    const uint8_t zf1 = zv1 ? ldv(a.zff + int64_t(zs1) * 128 + fidx) : uint8_t(0);
+    const T zr0 = zv0 ? ldv(zf + zo0) : T(0), zr1 = zv1 ? ldv(zf + zo1) : T(0);
+    const T zq0 = (zv0 && !first) ? ldv(zf + zo0 + 128 * qold) : T(0);
+    const T zq1 = (zv1 && !first) ? ldv(zf + zo1 + 128 * qold) : T(0);
+    Col<T> P, H;
 #pragma unroll
     for (int z = 0; z < 8; ++z) {
-      const uint8_t g = fbyte(f, z);
-      const T ap = stencil_z<T>(z, P, g, xm, xp, yh, zm, zp, lane);
-      if (g & 1) dp.add(P.v[z], ap);
+      P.v[z] = pnew_of<T>(fbyte(f, z), rc.v[z], first ? T(0) : pc.v[z], beta, first);
+      H.v[z] = hv ? pnew_of<T>(fbyte(hf, z), hr.v[z], first ? T(0) : hp.v[z], beta, first) : T(0);
     }
+    const T zm = pnew_of<T>(zf0, zr0, zq0, beta, first);
+    const T zp = pnew_of<T>(zf1, zr1, zq1, beta, first);
+    stcol(pnew, base + h.c, P);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + fidx;
+      zw[0] = P.v[0];
+      zw[64] = P.v[7];
+    }
+    __syncwarp();  // previous half leaf's tile reads are done
+    st_col_sh(tile.c[h.lx + 1][h.cy + 1], P);
+    if (h.lx != 2) st_col_sh(tile.c[h.tx][h.ty], H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, h.lx, h.cy, P, f, zm, zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z)
+      if (fbyte(f, z) & 1) dp.add(P.v[z], ap.v[z]);
   }
   double v[1] = {dp.value()};
   double tot[1];
@@ -530,6 +613,7 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_update(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
   const PcgScalars* sc = a.sc;
   if (sc->done) {
     // stop flag already set (converged at setup, or breakdown in spmv):
@@ -544,6 +628,7 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   T* x = static_cast<T*>(a.x);
   T* r = static_cast<T*>(a.r);
   const int lane = threadIdx.x & 31;
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
   const int wpb = kHotThreads / 32;
   Dot<DM> drr, drz;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
@@ -551,38 +636,51 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
   for (; hw < nhw; hw += hstride) {
     const int nbl_next = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
-    const HalfLeaf h = half_leaf(hw, lane);
-    const int64_t base = int64_t(h.s) * 512;
-    const uint2 f = ldflags(a.flags, base + h.c);
-    Col<T> P;
-    ldcol(p, base + h.c, P);
     int fs[6];
     face_slots(nbl, fs);
     nbl = nbl_next;
-    Col<T> xm, xp, yh;
-    if (h.lx == 0)
-      ld_pcol(a, h.xb == 0 ? fs[0] : h.s, ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3), p, xm);
-    if (h.lx == 3)
-      ld_pcol(a, h.xb == 0 ? h.s : fs[1], ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3), p, xp);
-    if (h.cy == 0 || h.cy == 7)
-      ld_pcol(a, h.cy == 0 ? fs[2] : fs[3], (h.cx << 6) | ((h.cy == 0 ? 7 : 0) << 3), p, yh);
-    const T zm = ld_pone(a, fs[4], h.c | 7, p), zp = ld_pone(a, fs[5], h.c, p);
-    Col<T> xc, rc;
+    const HalfLeaf h = half_leaf(hw, lane, fs);
+    const int64_t base = int64_t(h.s) * 512;
+    const uint2 f = ldflags(a.flags, base + h.c);
+    Col<T> P, H, xc, rc;
+    ldcol(p, base + h.c, P);
+    const bool hv = h.hslot >= 0 && h.hslot < a.n_pleaf;
+    if (hv) {
+      ldcol(p, int64_t(h.hslot) * 512 + h.hvox, H);
+    } else {
+#pragma unroll
+      for (int z = 0; z < 8; ++z) H.v[z] = T(0);
+    }
+    const int zs0 = fs[4], zs1 = fs[5];
+    const int fidx = (h.xb + h.lx) * 8 + h.cy;
+    const T* zfp = static_cast<const T*>(a.zf) + 128 * (1 + (it & 1)) + fidx;
+    const T zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? ldv(zfp + int64_t(zs0) * 384 + 64) : T(0);
+    const T zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + int64_t(zs1) * 384) : T(0);
     ldcol(x, base + h.c, xc);
     ldcol(r, base + h.c, rc);
+    __syncwarp();
+    st_col_sh(tile.c[h.lx + 1][h.cy + 1], P);
+    if (h.lx != 2) st_col_sh(tile.c[h.tx][h.ty], H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, h.lx, h.cy, P, f, zm, zp, ap);
 #pragma unroll
     for (int z = 0; z < 8; ++z) {
       const uint8_t g = fbyte(f, z);
-      const T ap = stencil_z<T>(z, P, g, xm, xp, yh, zm, zp, lane);
       xc.v[z] = tadd(tmul(alpha, P.v[z]), xc.v[z]);
-      rc.v[z] = tadd(tmul(nalpha, ap), rc.v[z]);
+      rc.v[z] = tadd(tmul(nalpha, ap.v[z]), rc.v[z]);
       if (g & 1) {
         drr.add(rc.v[z], rc.v[z]);
-        drz.add(rc.v[z], tmul(inv_diag<T>(g), rc.v[z]));
+        drz.add(rc.v[z], tmul(inv_sel<T>(g), rc.v[z]));
       }
     }
     stcol(x, base + h.c, xc);
     stcol(r, base + h.c, rc);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + fidx;
+      zw[0] = rc.v[0];
+      zw[64] = rc.v[7];
+    }
   }
   double v[2] = {drr.value(), drz.value()};
   double tot[2];
@@ -756,7 +854,7 @@ int ensure_pcg_vectors(fsim_sim* s, int precision) {
     FSIM_CK(s, cudaMalloc(&s->r64, n * sizeof(double)));
     FSIM_CK(s, cudaMalloc(&s->p64[0], n * sizeof(double)));
     FSIM_CK(s, cudaMalloc(&s->p64[1], n * sizeof(double)));
-    FSIM_CK(s, cudaMalloc(&s->Ap64, n * sizeof(double)));
+    FSIM_CK(s, cudaMalloc(&s->zface64, size_t(s->cap_pleaf) * 384 * sizeof(double)));
   }
   return FSIM_OK;
 }
@@ -780,7 +878,8 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st) {
   a.flags = s->flags;
   a.sc = s->d_sc;
   a.part = s->d_part;
-  a.Ap = s->Ap;
+  a.zf = s->zface;
+  a.zff = s->zflags;
   a.p0 = s->p[0];
   a.p1 = s->p[1];
   a.r = s->r;
@@ -808,7 +907,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st) {
       a.r = s->r64;
       a.p0 = s->p64[0];
       a.p1 = s->p64[1];
-      a.Ap = s->Ap64;
+      a.zf = s->zface64;
     }
     *s->h_sc = h;
     FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,

@@ -209,11 +209,13 @@ def test_fused_equals_staged_gpu():
     pb, vb, gb = b.download_particles()
     assert np.array_equal(pa, pb)
     assert rel_l2(va, vb) <= 1e-6 and rel_l2(ga, gb) <= 1e-6
+    # P2G sums in shared-memory atomic order, so the two runs differ at
+    # rounding level; 40 PCG iterations amplify that to ~1e-6: compare at the bar
     for fld in (fsim.FIELD_VELOCITY, fsim.FIELD_VELOCITY_UPDATE, fsim.FIELD_PRESSURE):
         x, xa = a.field(fld)
         y, ya = b.field(fld)
         assert np.array_equal(xa, ya)
-        assert rel_l2(x, y) <= 1e-6
+        assert rel_l2(x, y) <= FIELD_RTOL
     a.close()
     b.close()
 
