@@ -105,6 +105,7 @@ _SIGS = {
                                         C.POINTER(C.c_int32)]),
     "fsim_reset_kernel_times": (C.c_int, [_P]),
     "fsim_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "fsim_cfl_noalloc": (C.c_int, [_P, _P, C.POINTER(C.c_int32), C.c_float, _P, _P]),
 }
 
 _lib = None

@@ -242,6 +242,28 @@ int fsim_download_marker(fsim_t* sim, int32_t* out, uint8_t* active);
 int fsim_download_leaves(fsim_t* sim, int32_t* origins, int64_t capacity,
                          int64_t* n);
 
+/* ---- allocation-free CFL ---------------------------------------------- */
+/* No counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc while they step -- an engine that hands the solver device
+ * buffers from its own pre-reserved pool and forbids allocation in its frame
+ * loop, or a real-time loop where an allocation would stall the device.
+ * Computes FlipSimulation::CFL() (1/v, v = max(sqrt(0.5*gravity), max |v_d|
+ * over active in-box faces, excluding the last index on tangential axes),
+ * v >= 1e-2) from a face-velocity field the caller already holds in device
+ * memory, in the dense layout of fsim_download_field: vel has
+ * 3*(N1+2)(N2+2)(N3+2) floats, active one byte per voxel; the result is
+ * written to the device float *inv_speed, ordered on stream (NULL: the
+ * legacy default stream).  No handle; nothing is allocated: the reduction's
+ * scratch is a fixed file-scope device array (4 KB + a counter) that every
+ * GPU loading the library holds until exit.  The first call on a device
+ * looks up that array's address (cudaGetSymbolAddress) with the device
+ * current, so make the first call before any stream capture.  All calls on
+ * a device share the scratch: calls that overlap on the GPU race.
+ * Returns FSIM_ERR_CAPACITY when a dimension exceeds 1024 (the maximum),
+ * FSIM_ERR_INVALID for a null pointer or a dimension below 8. */
+int fsim_cfl_noalloc(const float* vel, const uint8_t* active, const int32_t dims[3],
+                     float gravity, float* inv_speed, void* stream);
+
 /* ---- kernel timing (CUDA events on the handle's stream) --------------- */
 int fsim_set_profiling(fsim_t* sim, int32_t enabled);
 /* Accumulated per-kernel device time since the last reset.  Writes up to
