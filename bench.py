@@ -327,6 +327,117 @@ def cpu_sample(args, iters_per_step=None):
     return t_step, npart, how
 
 
+def pcg_compare(args):
+    """Mixed-precision vs FP32 PCG on one divergence (the 512^3 multi-dam).
+
+    Runs one step to build the system, then solves it again with: an FP64
+    PCG to relative residual 1e-12 (the reference solution x64; the GPU FP64
+    path is checked against the FP64 oracle solve in tests/test_gpu_pcg.py),
+    plain FP32 PCG and MIXED PCG (FP32 inner iterations with FP64-accumulated
+    dots, FP64 outer residual refinement) at a ladder of tolerances.  Each
+    solve is timed with CUDA events on the library's stream; its error is
+    ||x - x64|| / ||x64|| over the fluid cells.  Prints one JSON line.
+    """
+    import torch
+
+    import fsim
+
+    wl = WORKLOADS[args.workload]
+    sim = make_sim(wl, args, 0)
+    stream = torch.cuda.ExternalStream(sim.stream(), device=0)
+    st = sim.step(0.01, fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 3000, tolerance=1e-5))
+    rows = st.pcg.n_rows
+
+    def solve(prm):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stt = sim.pcg_solve(prm)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        x, act = sim.field(fsim.FIELD_PRESSURE)
+        return e0.elapsed_time(e1), stt, x[act.astype(bool)].astype(np.float64)
+
+    t_ref, st_ref, xref = solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP64, 40000,
+                                                tolerance=1e-12))
+    nref = np.linalg.norm(xref)
+    out = {"metric": "PCG time to relative error vs FP64 solution", "unit": "ms",
+           "workload": args.workload, "unknowns": rows,
+           "fp64_reference": {"ms": t_ref, "iterations": st_ref.iterations,
+                              "rel_residual": float(np.sqrt(st_ref.rr / st_ref.bb))},
+           "fp32": [], "mixed": [], "fp64": []}
+    for tol in (1e-5, 1e-6, 1e-7, 1e-8):
+        ms, stt, x = solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 40000,
+                                           tolerance=tol))
+        out["fp32"].append({"tol": tol, "ms": ms, "iterations": stt.iterations,
+                            "status": stt.status, "error": float(np.linalg.norm(x - xref) / nref)})
+    for tol, inner in ((1e-6, 1e-2), (1e-7, 1e-2), (1e-8, 1e-3), (1e-9, 1e-3)):
+        ms, stt, x = solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 40000,
+                                           tolerance=tol, inner_tolerance=inner,
+                                           max_refinements=20))
+        out["mixed"].append({"tol": tol, "inner": inner, "ms": ms, "iterations": stt.iterations,
+                             "refinements": stt.refinements, "status": stt.status,
+                             "error": float(np.linalg.norm(x - xref) / nref)})
+
+    for tol in (1e-5, 1e-6, 1e-7):
+        ms, stt, x = solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP64, 40000,
+                                           tolerance=tol))
+        out["fp64"].append({"tol": tol, "ms": ms, "iterations": stt.iterations,
+                            "status": stt.status, "error": float(np.linalg.norm(x - xref) / nref)})
+
+    def best(lst):
+        ok = [r for r in lst if r["error"] <= 1e-6]
+        return min(ok, key=lambda r: r["ms"]) if ok else None
+
+    bf, bm, bd = best(out["fp32"]), best(out["mixed"]), best(out["fp64"])
+    out["fp32_error_floor"] = min(r["error"] for r in out["fp32"])
+    out["fastest_fp32_at_1e-6"] = bf
+    out["fastest_mixed_at_1e-6"] = bm
+    out["fastest_fp64_at_1e-6"] = bd
+    out["speedup_mixed_vs_fp32"] = (bf["ms"] / bm["ms"]) if (bf and bm) else None
+    out["speedup_mixed_vs_fp64"] = (bd["ms"] / bm["ms"]) if (bd and bm) else None
+    print(json.dumps(out))
+    sim.close()
+
+
+def pcg_micro(args):
+    """Per-kernel times of the PCG iteration on one step's pressure system.
+
+    One fsim_step builds the system (fp32, relative 1e-5).  Then the same
+    system is solved again with FSIM_PCG_FIXED for --micro-iters iterations:
+    once per precision with the library's CUDA-event profiling on (mean time
+    per launch of each kernel), and once without profiling (the graph loop;
+    wall time per iteration).  Prints one JSON line.  This is the program the
+    PCG ncu captures run.
+    """
+    import fsim
+
+    wl = WORKLOADS[args.workload]
+    sim = make_sim(wl, args, 0)
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 1500, tolerance=1e-5)
+    st = sim.step(0.01, prm)
+    k = args.micro_iters
+    out = {"workload": args.workload, "unknowns": st.pcg.n_rows, "step_iterations": st.pcg.iterations,
+           "fixed_iterations": k}
+    for prec, name in ((fsim.PREC_FP32, "fp32"), (fsim.PREC_MIXED, "mixed")):
+        sim.set_profiling(True)
+        sim.reset_kernel_times()
+        sim.pcg_solve(fsim.pcg_params(fsim.PCG_FIXED, prec, k))
+        sim.synchronize()
+        kt = sim.kernel_times()
+        sim.set_profiling(False)
+        out[name + "_us_per_launch"] = {n: round(v[0] / max(v[1], 1) * 1e3, 2)
+                                        for n, v in kt.items() if v[1] >= k // 2}
+    for prec, name in ((fsim.PREC_FP32, "fp32"), (fsim.PREC_MIXED, "mixed")):
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.pcg_solve(fsim.pcg_params(fsim.PCG_FIXED, prec, k))
+        sim.synchronize()
+        out[name + "_graph_us_per_iteration"] = round((time.perf_counter() - t0) / k * 1e6, 2)
+    print(json.dumps(out))
+    sim.close()
+
+
 def fsim_dt(inv, t_in):
     from oracle.oracle import compute_dt
 
@@ -350,6 +461,11 @@ def main():
     ap.add_argument("--cpu-pcg-iters", type=int, default=40)
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--pcg-compare", action="store_true",
+                    help="mixed vs FP32 PCG time to 1e-6 error (use --workload multidam_512)")
+    ap.add_argument("--pcg-micro", action="store_true",
+                    help="per-kernel PCG times on one step's system (fixed iteration count)")
+    ap.add_argument("--micro-iters", type=int, default=300)
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -360,6 +476,13 @@ def main():
               "cfl": 1, "flip": 0.95, "frame_rate": 30,
               "l2": "inputs larger than L2 (particle state > 129 MB)",
               "parallelism": f"replicas x{world}"}
+
+    if args.pcg_compare:
+        pcg_compare(args)
+        return
+    if args.pcg_micro:
+        pcg_micro(args)
+        return
 
     if args.impl == "reference":
         if rank != 0:

@@ -220,6 +220,7 @@ struct PcgArgs {
   PcgScalars* sc;
   double* part;
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
+  int par;          // spmv / update: parity of the iteration this launch serves
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
 };
 
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
       }
       a.flags[o] = f;
       x[o] = T(0);
+      static_cast<T*>(a.p1)[o] = T(0);  // p_old of the first iteration
       T rv;
       if (a.init_r) {
         rv = (f & 1) ? T(a.b[o]) : T(0);
@@ -279,6 +281,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
         const int fi = (cz == 7 ? 64 : 0) + cx * 8 + cy;
         a.zff[int64_t(s) * 128 + fi] = f;
         static_cast<T*>(a.zf)[int64_t(s) * 384 + fi] = rv;
+        static_cast<T*>(a.zf)[int64_t(s) * 384 + 256 + fi] = T(0);
       }
       const T z = tmul(inv_diag<T>(f), rv);
       drr.add(rv, rv);
@@ -364,13 +367,6 @@ __device__ __forceinline__ uint8_t fbyte(uint2 f, int z) {
   return uint8_t((z < 4 ? f.x : f.y) >> (8 * (z & 3)));
 }
 
-
-
-
-
-__device__ __forceinline__ float shfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-__device__ __forceinline__ double shfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
-
 // The six face-neighbour slots of a leaf, gathered by lanes 0..5 and
 // broadcast: 0 -x, 1 +x, 2 -y, 3 +y, 4 -z, 5 +z.  face_slot_lane loads the
 // lane's entry (issued one half leaf ahead); face_slots broadcasts them.
@@ -396,40 +392,37 @@ __device__ __forceinline__ void face_slots(int mine, int out[6]) {
 // per-warp shared tile [x: xb-1..xb+4][y: -1..8][z: 0..7]; each lane then
 // reads its four x/y neighbour columns with 16 B shared loads.
 struct HalfLeaf {
-  int s, xb, lx, cy, c;
-  int hslot, hvox;  // halo column (leaf slot, first voxel); hslot -1: none
-  int tx, ty;       // halo column position in the tile
+  int s, xb, lx, cy, c, fidx;
+  int tx, ty;  // halo column position in the tile
 };
-__device__ __forceinline__ HalfLeaf half_leaf(int hw, int lane, const int fs[6]) {
+__device__ __forceinline__ HalfLeaf half_pos(int hw, int lane) {
   HalfLeaf h;
   h.s = hw >> 1;
   h.xb = (hw & 1) * 4;
   h.lx = lane >> 3;
   h.cy = lane & 7;
   h.c = ((h.xb + h.lx) << 6) | (h.cy << 3);
-  h.hslot = -1;
-  h.hvox = 0;
-  h.tx = 0;
-  h.ty = 0;
+  h.fidx = (h.xb + h.lx) * 8 + h.cy;  // index of the column in a z-face plane
+  h.tx = h.lx == 0 ? 0 : (h.lx == 3 ? 5 : (h.cy & 3) + 1);
+  h.ty = h.lx == 1 ? (h.cy < 4 ? 0 : 9) : h.cy + 1;
+  return h;
+}
+// The lane's halo column: leaf slot (-1: none) and first voxel.
+__device__ __forceinline__ void halo_col(const HalfLeaf& h, const int fs[6], int& hslot,
+                                         int& hvox) {
+  hslot = -1;
+  hvox = 0;
   if (h.lx == 0) {
-    h.hslot = h.xb == 0 ? fs[0] : h.s;
-    h.hvox = ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3);
-    h.tx = 0;
-    h.ty = h.cy + 1;
+    hslot = h.xb == 0 ? fs[0] : h.s;
+    hvox = ((h.xb == 0 ? 7 : 3) << 6) | (h.cy << 3);
   } else if (h.lx == 3) {
-    h.hslot = h.xb == 0 ? h.s : fs[1];
-    h.hvox = ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3);
-    h.tx = 5;
-    h.ty = h.cy + 1;
+    hslot = h.xb == 0 ? h.s : fs[1];
+    hvox = ((h.xb == 0 ? 4 : 0) << 6) | (h.cy << 3);
   } else if (h.lx == 1) {
     const bool lo = h.cy < 4;
-    const int hx = h.cy & 3;
-    h.hslot = lo ? fs[2] : fs[3];
-    h.hvox = ((h.xb + hx) << 6) | ((lo ? 7 : 0) << 3);
-    h.tx = hx + 1;
-    h.ty = lo ? 0 : 9;
+    hslot = lo ? fs[2] : fs[3];
+    hvox = ((h.xb + (h.cy & 3)) << 6) | ((lo ? 7 : 0) << 3);
   }
-  return h;
 }
 
 // Jacobi inverse diagonal T(1.0/diag) by an exact select chain (pure ALU);
@@ -448,32 +441,46 @@ __device__ __forceinline__ T inv_sel(uint8_t f) {
   return (f & 1) ? v : T(0);
 }
 
+// {T(diag), T(1.0/diag)} by flags & 15 (bit 0 FLUID, bits 1-3 diag): the
+// values of flag_diag and inv_sel, read from shared memory in one load
+// instead of a compare/select chain per cell.
+template <typename T>
+struct __align__(2 * sizeof(T)) DiagInv {
+  T d, inv;
+};
+template <typename T>
+__device__ __forceinline__ void fill_diag_table(DiagInv<T>* tab) {
+  if (threadIdx.x < 16) {
+    const uint8_t f = uint8_t(threadIdx.x);
+    tab[threadIdx.x].d = T(flag_diag(f));
+    tab[threadIdx.x].inv = inv_sel<T>(f);
+  }
+}
+
+// Per-warp tile of p_j columns, stored as 16 B chunk planes
+// [chunk][x - xb + 1][y + 1]: the lanes of a quarter warp (consecutive y)
+// touch consecutive 16 B words, so tile loads and stores are conflict-free.
 template <typename T>
 struct __align__(16) Tile {
-  T c[6][10][8];  // [x - xb + 1][y + 1][z]; 16 B aligned for vector access
+  static constexpr int kV = int(sizeof(T)) / 2;  // 16 B chunks per 8-cell column
+  uint4 c[kV][6][10];
 };
 
-__device__ __forceinline__ void st_col_sh(float* p, const Col<float>& c) {
-  reinterpret_cast<float4*>(p)[0] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
-  reinterpret_cast<float4*>(p)[1] = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
-}
-__device__ __forceinline__ void st_col_sh(double* p, const Col<double>& c) {
+template <typename T>
+__device__ __forceinline__ void st_col_sh(Tile<T>& t, int x, int y, const Col<T>& c) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    reinterpret_cast<double2*>(p)[k] = make_double2(c.v[2 * k], c.v[2 * k + 1]);
+  for (int k = 0; k < Tile<T>::kV; ++k) {
+    uint4 u;
+    memcpy(&u, &c.v[k * (16 / sizeof(T))], 16);
+    t.c[k][x][y] = u;
+  }
 }
-__device__ __forceinline__ void ld_col_sh(const float* p, Col<float>& c) {
-  const float4 a = reinterpret_cast<const float4*>(p)[0];
-  const float4 b = reinterpret_cast<const float4*>(p)[1];
-  c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
-  c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
-}
-__device__ __forceinline__ void ld_col_sh(const double* p, Col<double>& c) {
+template <typename T>
+__device__ __forceinline__ void ld_col_sh(const Tile<T>& t, int x, int y, Col<T>& c) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const double2 a = reinterpret_cast<const double2*>(p)[k];
-    c.v[2 * k] = a.x;
-    c.v[2 * k + 1] = a.y;
+  for (int k = 0; k < Tile<T>::kV; ++k) {
+    const uint4 u = t.c[k][x][y];
+    memcpy(&c.v[k * (16 / sizeof(T))], &u, 16);
   }
 }
 
@@ -481,13 +488,14 @@ __device__ __forceinline__ void ld_col_sh(const double* p, Col<double>& c) {
 // (-x,-y,-z, diag, +z,+y,+x); 0 off-fluid.  The four x/y neighbour columns
 // come from the tile; zm / zp are the -z / +z face cells.
 template <typename T>
-__device__ __forceinline__ void stencil_col(const Tile<T>& t, int lx, int cy, const Col<T>& P,
-                                            uint2 f, T zm, T zp, Col<T>& out) {
+__device__ __forceinline__ void stencil_col(const Tile<T>& t, const DiagInv<T>* tab, int lx,
+                                            int cy, const Col<T>& P, uint2 f, T zm, T zp,
+                                            Col<T>& out) {
   Col<T> xm, xp, ym, yp;
-  ld_col_sh(t.c[lx][cy + 1], xm);
-  ld_col_sh(t.c[lx + 2][cy + 1], xp);
-  ld_col_sh(t.c[lx + 1][cy], ym);
-  ld_col_sh(t.c[lx + 1][cy + 2], yp);
+  ld_col_sh(t, lx, cy + 1, xm);
+  ld_col_sh(t, lx + 2, cy + 1, xp);
+  ld_col_sh(t, lx + 1, cy, ym);
+  ld_col_sh(t, lx + 1, cy + 2, yp);
 #pragma unroll
   for (int z = 0; z < 8; ++z) {
     const uint8_t g = fbyte(f, z);
@@ -496,7 +504,7 @@ __device__ __forceinline__ void stencil_col(const Tile<T>& t, int lx, int cy, co
     acc = tsub(acc, xm.v[z]);
     acc = tsub(acc, ym.v[z]);
     acc = tsub(acc, vzm);
-    acc = tadd(acc, tmul(T(flag_diag(g)), P.v[z]));
+    acc = tadd(acc, tmul(tab[g & 15].d, P.v[z]));
     acc = tsub(acc, vzp);
     acc = tsub(acc, yp.v[z]);
     acc = tsub(acc, xp.v[z]);
@@ -504,14 +512,19 @@ __device__ __forceinline__ void stencil_col(const Tile<T>& t, int lx, int cy, co
   }
 }
 
-// p = z + beta p_old with z = r/diag (p = z at the first iteration); 0 off-fluid
+// p = z + beta p_old with z = r/diag.  Off-fluid both terms are 0 (the
+// table's inverse is 0 there and r, p are stored 0), and at the first
+// iteration beta = 0 and p_old was zeroed by the setup, so no select is needed.
 template <typename T>
-__device__ __forceinline__ T pnew_of(uint8_t f, T r, T po, T beta, bool first) {
-  const T z = tmul(inv_sel<T>(f), r);
-  const T v = first ? z : tadd(z, tmul(beta, po));
-  return (f & 1) ? v : T(0);
+__device__ __forceinline__ T pnew_of(const DiagInv<T>* tab, uint8_t f, T r, T po, T beta) {
+  return tadd(tmul(tab[f & 15].inv, r), tmul(beta, po));
 }
 
+// Each launch of the hot kernels serves one iteration of known parity
+// (PcgArgs::par), so its buffers are fixed before the device scalars are
+// read: the first half leaf's own-column loads are issued together with the
+// loads of the stop flag and the step scalars.
+//
 // p_j = z_j + beta_{j-1} p_{j-1} on the half leaf and its halo (z = r/diag
 // recomputed, never stored), then p_j.(A p_j); the last CTA forms alpha_j.
 // Only p_j is written: the update kernel recomputes A p_j from it.
@@ -519,80 +532,101 @@ template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_spmv(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
-  const PcgScalars* sc = a.sc;
-  if (sc->done) return;
-  const int it = sc->iter;
-  const bool first = it == 0;
-  const T beta = T(sc->beta);
+  __shared__ DiagInv<T> tab[16];
+  const int par = a.par;
   const T* r = static_cast<const T*>(a.r);
-  const T* pold = static_cast<const T*>((it & 1) ? a.p0 : a.p1);
-  T* pnew = static_cast<T*>((it & 1) ? a.p1 : a.p0);
+  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
+  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
+  const int qold = 1 + (par ^ 1), qnew = 1 + par;
   const int lane = threadIdx.x & 31;
-  Tile<T>& tile = tiles[threadIdx.x >> 5];
   const int wpb = kHotThreads / 32;
-  Dot<DM> dp;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  // first half leaf: own column and face slots, in flight with the scalars
+  Col<T> rc, pc;
+  uint2 f = make_uint2(0u, 0u);
+  if (hw < nhw) {
+    const HalfLeaf h0 = half_pos(hw, lane);
+    const int64_t o = int64_t(h0.s) * 512 + h0.c;
+    f = ldflags(a.flags, o);
+    ldcol(r, o, rc);
+    ldcol(pold, o, pc);
+  }
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  const PcgScalars* sc = a.sc;
+  const int done = sc->done;
+  const T beta = T(sc->beta);
+  fill_diag_table<T>(tab);
+  __syncthreads();
+  if (done) return;
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
+  Dot<DM> dp;
   for (; hw < nhw; hw += hstride) {
     const int nbl_next = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
     int fs[6];
     face_slots(nbl, fs);
     nbl = nbl_next;
-    const HalfLeaf h = half_leaf(hw, lane, fs);
-    const int64_t base = int64_t(h.s) * 512;
-    // own column
-    const uint2 f = ldflags(a.flags, base + h.c);
-    Col<T> rc, pc;
-    ldcol(r, base + h.c, rc);
-    if (!first) ldcol(pold, base + h.c, pc);
+    const HalfLeaf h = half_pos(hw, lane);
+    int hslot, hvox;
+    halo_col(h, fs, hslot, hvox);
     // halo column
-    const bool hv = h.hslot >= 0 && h.hslot < a.n_pleaf;
-    const int64_t hb = int64_t(hv ? h.hslot : 0) * 512 + h.hvox;
+    const bool hv = hslot >= 0 && hslot < a.n_pleaf;
+    const int64_t hb = int64_t(hv ? hslot : 0) * 512 + hvox;
     uint2 hf = make_uint2(0u, 0u);
     Col<T> hr, hp;
     if (hv) {
       hf = ldflags(a.flags, hb);
       ldcol(r, hb, hr);
-      if (!first) ldcol(pold, hb, hp);
+      ldcol(pold, hb, hp);
+    } else {
+#pragma unroll
+      for (int z = 0; z < 8; ++z) hr.v[z] = hp.v[z] = T(0);
     }
     // z faces of the own column, from the neighbours' published planes:
     // the -z leaf's z=7 plane and the +z leaf's z=0 plane
     const int zs0 = fs[4], zs1 = fs[5];
     const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
-    const int fidx = (h.xb + h.lx) * 8 + h.cy;
     const T* zf = static_cast<const T*>(a.zf);
-    const int qold = 1 + ((it + 1) & 1), qnew = 1 + (it & 1);
-    const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + fidx;
-    const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + fidx;
-    const uint8_t zf0 = zv0 ? ldv(a.zff + int64_t(zs0) * 128 + 64 + fidx) : uint8_t(0);
-    const uint8_t zf1 = zv1 ? ldv(a.zff + int64_t(zs1) * 128 + fidx) : uint8_t(0);
+    const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + h.fidx;
+    const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + h.fidx;
+    const uint8_t zf0 = zv0 ? ldv(a.zff + int64_t(zs0) * 128 + 64 + h.fidx) : uint8_t(0);
+    const uint8_t zf1 = zv1 ? ldv(a.zff + int64_t(zs1) * 128 + h.fidx) : uint8_t(0);
     const T zr0 = zv0 ? ldv(zf + zo0) : T(0), zr1 = zv1 ? ldv(zf + zo1) : T(0);
-    const T zq0 = (zv0 && !first) ? ldv(zf + zo0 + 128 * qold) : T(0);
-    const T zq1 = (zv1 && !first) ? ldv(zf + zo1 + 128 * qold) : T(0);
+    const T zq0 = zv0 ? ldv(zf + zo0 + 128 * qold) : T(0);
+    const T zq1 = zv1 ? ldv(zf + zo1 + 128 * qold) : T(0);
     Col<T> P, H;
 #pragma unroll
     for (int z = 0; z < 8; ++z) {
-      P.v[z] = pnew_of<T>(fbyte(f, z), rc.v[z], first ? T(0) : pc.v[z], beta, first);
-      H.v[z] = hv ? pnew_of<T>(fbyte(hf, z), hr.v[z], first ? T(0) : hp.v[z], beta, first) : T(0);
+      P.v[z] = pnew_of<T>(tab, fbyte(f, z), rc.v[z], pc.v[z], beta);
+      H.v[z] = pnew_of<T>(tab, fbyte(hf, z), hr.v[z], hp.v[z], beta);
     }
-    const T zm = pnew_of<T>(zf0, zr0, zq0, beta, first);
-    const T zp = pnew_of<T>(zf1, zr1, zq1, beta, first);
-    stcol(pnew, base + h.c, P);
+    const T zm = pnew_of<T>(tab, zf0, zr0, zq0, beta);
+    const T zp = pnew_of<T>(tab, zf1, zr1, zq1, beta);
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    stcol(pnew, o, P);
     {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + fidx;
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
       zw[0] = P.v[0];
       zw[64] = P.v[7];
     }
     __syncwarp();  // previous half leaf's tile reads are done
-    st_col_sh(tile.c[h.lx + 1][h.cy + 1], P);
-    if (h.lx != 2) st_col_sh(tile.c[h.tx][h.ty], H);
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
     __syncwarp();
+    const uint2 fc = f;
+    // next half leaf's own column (registers of this one are free now)
+    if (hw + hstride < nhw) {
+      const HalfLeaf hn = half_pos(hw + hstride, lane);
+      const int64_t on = int64_t(hn.s) * 512 + hn.c;
+      f = ldflags(a.flags, on);
+      ldcol(r, on, rc);
+      ldcol(pold, on, pc);
+    }
     Col<T> ap;
-    stencil_col<T>(tile, h.lx, h.cy, P, f, zm, zp, ap);
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, fc, zm, zp, ap);
+    // off-fluid P and Ap are 0: their terms add exact zeros
 #pragma unroll
-    for (int z = 0; z < 8; ++z)
-      if (fbyte(f, z) & 1) dp.add(P.v[z], ap.v[z]);
+    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
   }
   double v[1] = {dp.value()};
   double tot[1];
@@ -614,72 +648,94 @@ template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_update(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  const int par = a.par;
+  const T* p = static_cast<const T*>(par ? a.p1 : a.p0);
+  T* x = static_cast<T*>(a.x);
+  T* r = static_cast<T*>(a.r);
+  const int qcur = 1 + par;
+  const int lane = threadIdx.x & 31;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  // first half leaf: own column and face slots, in flight with the scalars
+  Col<T> P, xc, rc;
+  uint2 f = make_uint2(0u, 0u);
+  if (hw < nhw) {
+    const HalfLeaf h0 = half_pos(hw, lane);
+    const int64_t o = int64_t(h0.s) * 512 + h0.c;
+    f = ldflags(a.flags, o);
+    ldcol(p, o, P);
+    ldcol(x, o, xc);
+    ldcol(r, o, rc);
+  }
+  int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
   const PcgScalars* sc = a.sc;
-  if (sc->done) {
+  const int done = sc->done;
+  const int it = sc->iter;
+  const T alpha = T(sc->alpha);
+  fill_diag_table<T>(tab);
+  __syncthreads();
+  if (done) {
     // stop flag already set (converged at setup, or breakdown in spmv):
     // end the graph's WHILE loop
     if (a.cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
     return;
   }
-  const int it = sc->iter;
-  const T alpha = T(sc->alpha);
   const T nalpha = -alpha;
-  const T* p = static_cast<const T*>((it & 1) ? a.p1 : a.p0);
-  T* x = static_cast<T*>(a.x);
-  T* r = static_cast<T*>(a.r);
-  const int lane = threadIdx.x & 31;
   Tile<T>& tile = tiles[threadIdx.x >> 5];
-  const int wpb = kHotThreads / 32;
   Dot<DM> drr, drz;
-  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
-  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
   for (; hw < nhw; hw += hstride) {
     const int nbl_next = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
     int fs[6];
     face_slots(nbl, fs);
     nbl = nbl_next;
-    const HalfLeaf h = half_leaf(hw, lane, fs);
-    const int64_t base = int64_t(h.s) * 512;
-    const uint2 f = ldflags(a.flags, base + h.c);
-    Col<T> P, H, xc, rc;
-    ldcol(p, base + h.c, P);
-    const bool hv = h.hslot >= 0 && h.hslot < a.n_pleaf;
+    const HalfLeaf h = half_pos(hw, lane);
+    int hslot, hvox;
+    halo_col(h, fs, hslot, hvox);
+    Col<T> H;
+    const bool hv = hslot >= 0 && hslot < a.n_pleaf;
     if (hv) {
-      ldcol(p, int64_t(h.hslot) * 512 + h.hvox, H);
+      ldcol(p, int64_t(hslot) * 512 + hvox, H);
     } else {
 #pragma unroll
       for (int z = 0; z < 8; ++z) H.v[z] = T(0);
     }
     const int zs0 = fs[4], zs1 = fs[5];
-    const int fidx = (h.xb + h.lx) * 8 + h.cy;
-    const T* zfp = static_cast<const T*>(a.zf) + 128 * (1 + (it & 1)) + fidx;
+    const T* zfp = static_cast<const T*>(a.zf) + 128 * qcur + h.fidx;
     const T zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? ldv(zfp + int64_t(zs0) * 384 + 64) : T(0);
     const T zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + int64_t(zs1) * 384) : T(0);
-    ldcol(x, base + h.c, xc);
-    ldcol(r, base + h.c, rc);
-    __syncwarp();
-    st_col_sh(tile.c[h.lx + 1][h.cy + 1], P);
-    if (h.lx != 2) st_col_sh(tile.c[h.tx][h.ty], H);
+    __syncwarp();  // previous half leaf's tile reads are done
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
     __syncwarp();
     Col<T> ap;
-    stencil_col<T>(tile, h.lx, h.cy, P, f, zm, zp, ap);
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, f, zm, zp, ap);
 #pragma unroll
     for (int z = 0; z < 8; ++z) {
       const uint8_t g = fbyte(f, z);
       xc.v[z] = tadd(tmul(alpha, P.v[z]), xc.v[z]);
       rc.v[z] = tadd(tmul(nalpha, ap.v[z]), rc.v[z]);
-      if (g & 1) {
-        drr.add(rc.v[z], rc.v[z]);
-        drz.add(rc.v[z], tmul(inv_sel<T>(g), rc.v[z]));
-      }
+      // off-fluid r is 0 (Ap is 0 there): the terms add exact zeros
+      drr.add(rc.v[z], rc.v[z]);
+      drz.add(rc.v[z], tmul(tab[g & 15].inv, rc.v[z]));
     }
-    stcol(x, base + h.c, xc);
-    stcol(r, base + h.c, rc);
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    stcol(x, o, xc);
+    stcol(r, o, rc);
     {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + fidx;
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + h.fidx;
       zw[0] = rc.v[0];
       zw[64] = rc.v[7];
+    }
+    // next half leaf's own column
+    if (hw + hstride < nhw) {
+      const HalfLeaf hn = half_pos(hw + hstride, lane);
+      const int64_t on = int64_t(hn.s) * 512 + hn.c;
+      f = ldflags(a.flags, on);
+      ldcol(p, on, P);
+      ldcol(x, on, xc);
+      ldcol(r, on, rc);
     }
   }
   double v[2] = {drr.value(), drz.value()};
@@ -752,8 +808,10 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
     pres[o] = float(x[o]);
 }
 
-// Builds and launches graph = WHILE(cond){ spmv; update } on the handle's
-// stream.  Returns FSIM_OK, or FSIM_ERR_CUDA when the graph API refuses
+// Builds and launches graph = WHILE(cond){ spmv; update; spmv; update } on
+// the handle's stream: one pass runs an even and an odd iteration (their
+// buffers are fixed by PcgArgs::par), and kernels launched after the stop
+// flag is set return at once.  Returns FSIM_OK, or FSIM_ERR_CUDA when the graph API refuses
 // (the caller then polls from the host).  Kernel launches inside the graph
 // are counted by the caller from the iteration count the solve reports.
 template <typename T, int DM>
@@ -773,18 +831,22 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid) {
   if (e == cudaSuccess) {
     cudaGraph_t body = np.conditional.phGraph_out[0];
     a.cond = h;
-    cudaKernelNodeParams kp;
-    memset(&kp, 0, sizeof(kp));
-    void* args[] = {&a};
-    kp.gridDim = dim3(unsigned(wgrid));
-    kp.blockDim = dim3(unsigned(kHotThreads));
-    kp.kernelParams = args;
-    cudaGraphNode_t n1 = nullptr, n2 = nullptr;
-    kp.func = reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
-    e = cudaGraphAddKernelNode(&n1, body, nullptr, 0, &kp);
-    if (e == cudaSuccess) {
-      kp.func = reinterpret_cast<void*>(k_pcg_update<T, DM>);
-      e = cudaGraphAddKernelNode(&n2, body, &n1, 1, &kp);
+    PcgArgs ap[2] = {a, a};
+    ap[0].par = 0;
+    ap[1].par = 1;
+    cudaGraphNode_t prev = nullptr;
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+      cudaKernelNodeParams kp;
+      memset(&kp, 0, sizeof(kp));
+      void* args[] = {&ap[k >> 1]};
+      kp.gridDim = dim3(unsigned(wgrid));
+      kp.blockDim = dim3(unsigned(kHotThreads));
+      kp.kernelParams = args;
+      kp.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
+                        : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+      cudaGraphNode_t n = nullptr;
+      e = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp);
+      prev = n;
     }
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
@@ -824,20 +886,24 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
-      // each WHILE pass runs both kernels; one pass follows a stop at setup
-      s->launches += 2 * int64_t(std::max(s->h_sc->iter + (s->h_sc->status ? 1 : 0), 1));
+      // each WHILE pass runs two iterations (four kernels); the pass that
+      // sees the stop flag at setup or after a breakdown also counts
+      const int64_t pairs = std::max(s->h_sc->iter + (s->h_sc->status ? 1 : 0), 1);
+      s->launches += 4 * ((pairs + 1) / 2);
       return FSIM_OK;
     }
     s->use_graphs = false;  // fall back for the rest of this handle's life
   }
   a.cond = 0;
   int chunk = 8;
+  int64_t launched = 0;  // iterations launched; the device count equals it until the stop
   for (;;) {
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                s->stream));
     FSIM_CK(s, cudaStreamSynchronize(s->stream));
     if (s->h_sc->done) break;
-    for (int c = 0; c < chunk; ++c) {
+    for (int c = 0; c < chunk; ++c, ++launched) {
+      a.par = int(launched & 1);
       FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kHotThreads, 0, a);
       FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kHotThreads, 0, a);
     }
