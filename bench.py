@@ -412,6 +412,8 @@ def pcg_micro(args):
     """
     import fsim
 
+    if args.lib:
+        fsim._lib = fsim.load_library(args.lib)  # a variant build of the library
     wl = WORKLOADS[args.workload]
     sim = make_sim(wl, args, 0)
     prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 1500, tolerance=1e-5)
@@ -434,6 +436,7 @@ def pcg_micro(args):
         sim.pcg_solve(fsim.pcg_params(fsim.PCG_FIXED, prec, k))
         sim.synchronize()
         out[name + "_graph_us_per_iteration"] = round((time.perf_counter() - t0) / k * 1e6, 2)
+    out["pcg_graph_mode"] = os.environ.get("FSIM_PCG_GRAPH", "1")
     print(json.dumps(out))
     sim.close()
 
@@ -466,6 +469,7 @@ def main():
     ap.add_argument("--pcg-micro", action="store_true",
                     help="per-kernel PCG times on one step's system (fixed iteration count)")
     ap.add_argument("--micro-iters", type=int, default=300)
+    ap.add_argument("--lib", default=None, help="--pcg-micro: path of a variant libfsim.so")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))

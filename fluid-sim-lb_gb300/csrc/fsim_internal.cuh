@@ -249,8 +249,10 @@ struct fsim_sim {
   bool weight_valid = false;
   bool deleted_outside = false;
 
-  // PCG iterations as a CUDA graph with a conditional WHILE node
+  // PCG iterations as a CUDA graph with a conditional WHILE node, its
+  // kernels joined by programmatic (early-launch) edges
   bool use_graphs = true;
+  bool use_pdl = false;
 
   // profiling
   bool profiling = false;

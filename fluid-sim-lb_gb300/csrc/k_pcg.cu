@@ -520,6 +520,17 @@ __device__ __forceinline__ T pnew_of(const DiagInv<T>* tab, uint8_t f, T r, T po
   return tadd(tmul(tab[f & 15].inv, r), tmul(beta, po));
 }
 
+// Programmatic dependent launch: a kernel launched with a programmatic edge
+// may start while its predecessor finishes.  Everything before pdl_wait()
+// reads only data the predecessor does not write; pdl_wait() returns once
+// the predecessor grid has completed and its writes are visible (at once
+// when there is no programmatic edge).  pdl_trigger() lets the successor
+// start launching.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 // Each launch of the hot kernels serves one iteration of known parity
 // (PcgArgs::par), so its buffers are fixed before the device scalars are
 // read: the first half leaf's own-column loads are issued together with the
@@ -542,21 +553,23 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  // first half leaf: own column and face slots, in flight with the scalars
+  // first half leaf: flags, p_{j-1} (written two launches back) and face
+  // slots before the wait; r and the scalars (written by the previous
+  // update) after it
   Col<T> rc, pc;
   uint2 f = make_uint2(0u, 0u);
+  const int64_t o0 = hw < nhw ? int64_t(hw >> 1) * 512 + half_pos(hw, lane).c : 0;
   if (hw < nhw) {
-    const HalfLeaf h0 = half_pos(hw, lane);
-    const int64_t o = int64_t(h0.s) * 512 + h0.c;
-    f = ldflags(a.flags, o);
-    ldcol(r, o, rc);
-    ldcol(pold, o, pc);
+    f = ldflags(a.flags, o0);
+    ldcol(pold, o0, pc);
   }
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  fill_diag_table<T>(tab);
+  pdl_wait();
   const PcgScalars* sc = a.sc;
   const int done = sc->done;
   const T beta = T(sc->beta);
-  fill_diag_table<T>(tab);
+  if (hw < nhw) ldcol(r, o0, rc);
   __syncthreads();
   if (done) return;
   Tile<T>& tile = tiles[threadIdx.x >> 5];
@@ -628,6 +641,7 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
 #pragma unroll
     for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
   }
+  pdl_trigger();
   double v[1] = {dp.value()};
   double tot[1];
   if (grid_sum<DM, 1, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
@@ -658,23 +672,24 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  // first half leaf: own column and face slots, in flight with the scalars
+  // first half leaf: flags, x, r (not written by the spmv) and face slots
+  // before the wait; p_j and the scalars after it
   Col<T> P, xc, rc;
   uint2 f = make_uint2(0u, 0u);
+  const int64_t o0 = hw < nhw ? int64_t(hw >> 1) * 512 + half_pos(hw, lane).c : 0;
   if (hw < nhw) {
-    const HalfLeaf h0 = half_pos(hw, lane);
-    const int64_t o = int64_t(h0.s) * 512 + h0.c;
-    f = ldflags(a.flags, o);
-    ldcol(p, o, P);
-    ldcol(x, o, xc);
-    ldcol(r, o, rc);
+    f = ldflags(a.flags, o0);
+    ldcol(x, o0, xc);
+    ldcol(r, o0, rc);
   }
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  fill_diag_table<T>(tab);
+  pdl_wait();
   const PcgScalars* sc = a.sc;
   const int done = sc->done;
   const int it = sc->iter;
   const T alpha = T(sc->alpha);
-  fill_diag_table<T>(tab);
+  if (hw < nhw) ldcol(p, o0, P);
   __syncthreads();
   if (done) {
     // stop flag already set (converged at setup, or breakdown in spmv):
@@ -738,6 +753,7 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
       ldcol(r, on, rc);
     }
   }
+  pdl_trigger();
   double v[2] = {drr.value(), drz.value()};
   double tot[2];
   if (grid_sum<DM, 2, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
@@ -808,14 +824,18 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
     pres[o] = float(x[o]);
 }
 
-// Builds and launches graph = WHILE(cond){ spmv; update; spmv; update } on
-// the handle's stream: one pass runs an even and an odd iteration (their
-// buffers are fixed by PcgArgs::par), and kernels launched after the stop
-// flag is set return at once.  Returns FSIM_OK, or FSIM_ERR_CUDA when the graph API refuses
+// Builds and launches graph = WHILE(cond){ (spmv; update) x kPassIters } on
+// the handle's stream: one pass runs kPassIters iterations of alternating
+// parity (their buffers are fixed by PcgArgs::par), and kernels launched
+// after the stop flag is set return at once.  With pdl the kernels of a
+// pass are joined by programmatic edges, so each one's prologue overlaps
+// its predecessor's reduction tail.  Returns FSIM_OK, or FSIM_ERR_CUDA when the graph API refuses
 // (the caller then polls from the host).  Kernel launches inside the graph
 // are counted by the caller from the iteration count the solve reports.
+constexpr int kPassIters = 4;  // PCG iterations per pass of the graph's WHILE body
+
 template <typename T, int DM>
-int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid) {
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -835,17 +855,23 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid) {
     ap[0].par = 0;
     ap[1].par = 1;
     cudaGraphNode_t prev = nullptr;
-    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
-      cudaKernelNodeParams kp;
-      memset(&kp, 0, sizeof(kp));
-      void* args[] = {&ap[k >> 1]};
-      kp.gridDim = dim3(unsigned(wgrid));
-      kp.blockDim = dim3(unsigned(kHotThreads));
-      kp.kernelParams = args;
-      kp.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
-                        : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+    for (int k = 0; k < 2 * kPassIters && e == cudaSuccess; ++k) {
+      cudaGraphNodeParams kn = {};
+      kn.type = cudaGraphNodeTypeKernel;
+      void* args[] = {&ap[(k >> 1) & 1]};
+      kn.kernel.gridDim = dim3(unsigned(wgrid));
+      kn.kernel.blockDim = dim3(unsigned(kHotThreads));
+      kn.kernel.kernelParams = args;
+      kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
+                               : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+      cudaGraphEdgeData ed = {};
+      if (pdl) {
+        ed.from_port = cudaGraphKernelNodePortProgrammatic;
+        ed.type = cudaGraphDependencyTypeProgrammatic;
+      }
       cudaGraphNode_t n = nullptr;
-      e = cudaGraphAddKernelNode(&n, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp);
+      e = cudaGraphAddNode(&n, body, prev ? &prev : nullptr, prev ? &ed : nullptr, prev ? 1 : 0,
+                           &kn);
       prev = n;
     }
   }
@@ -881,7 +907,12 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks}));
   if (s->use_graphs && !s->profiling) {
-    int rc = run_graph_loop<T, DM>(s, a, wgrid);
+    int rc = FSIM_ERR_CUDA;
+    if (s->use_pdl) {
+      rc = run_graph_loop<T, DM>(s, a, wgrid, true);
+      if (rc != FSIM_OK) s->use_pdl = false;  // programmatic edges refused: plain edges
+    }
+    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, false);
     if (rc == FSIM_OK) {
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
@@ -889,7 +920,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       // each WHILE pass runs two iterations (four kernels); the pass that
       // sees the stop flag at setup or after a breakdown also counts
       const int64_t pairs = std::max(s->h_sc->iter + (s->h_sc->status ? 1 : 0), 1);
-      s->launches += 4 * ((pairs + 1) / 2);
+      s->launches += 2 * kPassIters * ((pairs + kPassIters - 1) / kPassIters);
       return FSIM_OK;
     }
     s->use_graphs = false;  // fall back for the rest of this handle's life
