@@ -296,7 +296,10 @@ int launch_pressure_update(fsim_sim* s, bool fused);
 int launch_velocity_update(fsim_sim* s);
 int launch_cfl(fsim_sim* s);
 int launch_g2p(fsim_sim* s);
-int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st);
+// b64: an fp64 right-hand side on the particle-leaf cells instead of the
+// divergence (the solution is then read from x64: FP64 / MIXED precision)
+int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st,
+              const double* b64 = nullptr);
 int download_dense(fsim_sim* s, int field, float* out, uint8_t* active);
 int download_marker(fsim_sim* s, int32_t* out, uint8_t* active);
 int seed_fluid(fsim_sim* s, const fsim_seed_pass* passes, int npasses, uint64_t seed);

@@ -64,10 +64,23 @@ __device__ __forceinline__ bool in_box(const int n[3], int i, int j, int k) {
   return i >= 0 && j >= 0 && k >= 0 && i < n[0] && j < n[1] && k < n[2];
 }
 
+// P2G sums are accumulated in 64-bit fixed point (2^-32 units): integer
+// atomics commute, so the sums -- and every step -- are bitwise reproducible
+// whatever order the CTA's threads add in.  Each float term w*u (and w) is
+// converted exactly up to 2^-33; the result is then the correctly rounded
+// float of the exact sum of the terms.  Range: |sum| < 2^31 per face.
+constexpr float kFixScale = 4294967296.0f;  // 2^32
+__device__ __forceinline__ unsigned long long to_fix(float x) {
+  return static_cast<unsigned long long>(__float2ll_rn(__fmul_rn(x, kFixScale)));
+}
+__device__ __forceinline__ float from_fix(unsigned long long v) {
+  return float(double(static_cast<long long>(v)) * (1.0 / 4294967296.0));
+}
+
 template <bool FUSED>
 __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a) {
-  __shared__ float sv[3][512];
-  __shared__ float sw[3][512];
+  __shared__ unsigned long long sv[3][512];
+  __shared__ unsigned long long sw[3][512];
   __shared__ uint8_t touched[512];
   __shared__ int nb[27];
   const int s = blockIdx.x;
@@ -76,8 +89,8 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
   origin_of(a, s, org);
   if (tid < 27) nb[tid] = a.nbr[int64_t(s) * 27 + tid];
   for (int v = tid; v < 512; v += 256) {
-    sv[0][v] = 0.f; sv[1][v] = 0.f; sv[2][v] = 0.f;
-    sw[0][v] = 0.f; sw[1][v] = 0.f; sw[2][v] = 0.f;
+    sv[0][v] = 0ull; sv[1][v] = 0ull; sv[2][v] = 0ull;
+    sw[0][v] = 0ull; sw[1][v] = 0ull; sw[2][v] = 0ull;
     touched[v] = 0;
   }
   __syncthreads();
@@ -128,8 +141,8 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
               if ((unsigned)i < 8u && (unsigned)j < 8u && (unsigned)k < 8u) {
                 const int o = (i << 6) | (j << 3) | k;
                 const float ww = w[di][dj][dk];
-                atomicAdd(&sv[D][o], __fmul_rn(ww, u[D]));
-                atomicAdd(&sw[D][o], ww);
+                atomicAdd(&sv[D][o], to_fix(__fmul_rn(ww, u[D])));
+                atomicAdd(&sw[D][o], to_fix(ww));
                 touched[o] = 1;
               }
             }
@@ -144,11 +157,13 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
     const bool on = touched[v] != 0;
     float val[3];
 #pragma unroll
+    float wsum[3];
     for (int D = 0; D < 3; ++D) {
-      const float ws = sw[D][v];
+      const float ws = from_fix(sw[D][v]);
+      wsum[D] = ws;
       // THRESH is a double literal in the reference: float ws < 1e-5 (double)
       // is ws <= 1e-5f
-      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(sv[D][v], ws)) : 0.f;
+      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(from_fix(sv[D][v]), ws)) : 0.f;
     }
     // marker: FLUID for in-box cells holding particles
     bool has = false;
@@ -184,7 +199,7 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
 #pragma unroll
       for (int D = 0; D < 3; ++D) {
         vel[D * 512 + v] = val[D];
-        wt[D * 512 + v] = on ? sw[D][v] : 0.f;
+        wt[D * 512 + v] = on ? wsum[D] : 0.f;
       }
       // ClearGridData left the saved velocity empty
       if ((threadIdx.x & 31) == 0) a.vold_on[int64_t(s) * 16 + (v >> 5)] = 0u;

@@ -208,6 +208,7 @@ struct PcgArgs {
   const int32_t* nbr;
   const int8_t* marker;
   const float* b;   // divergence (fp32)
+  const double* b64;  // fp64 right-hand side instead of b (adjoint / replay solves), or null
   uint8_t* flags;
   void* x;
   void* r;
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
       static_cast<T*>(a.p1)[o] = T(0);  // p_old of the first iteration
       T rv;
       if (a.init_r) {
-        rv = (f & 1) ? T(a.b[o]) : T(0);
+        rv = (f & 1) ? (a.b64 ? T(a.b64[o]) : T(a.b[o])) : T(0);
         r[o] = rv;
       } else {
         rv = r[o];
@@ -807,7 +808,7 @@ __global__ void __launch_bounds__(kThreads) k_residual64(const __grid_constant__
         const int64_t u = int64_t(ns) * 512 + (((ux & 7) << 6) | ((uy & 7) << 3) | (uz & 7));
         if (a.flags[u] & 1) ax -= a.x64[u];
       }
-      const double res = double(a.b[o]) - ax;
+      const double res = (a.b64 ? a.b64[o] : double(a.b[o])) - ax;
       rr32[o] = float(res);
       acc += res * res;
     }
@@ -958,7 +959,7 @@ int ensure_pcg_vectors(fsim_sim* s, int precision) {
 
 }  // namespace
 
-int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st) {
+int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const double* b64) {
   if (!prm) return fail(s, FSIM_ERR_INVALID, "pcg params missing");
   if (prm->mode < 0 || prm->mode > 2 || prm->precision < 0 || prm->precision > 2)
     return fail(s, FSIM_ERR_INVALID, "bad pcg mode/precision");
@@ -972,6 +973,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st) {
   a.nbr = s->d_nbr;
   a.marker = s->marker;
   a.b = s->div;
+  a.b64 = b64;
   a.flags = s->flags;
   a.sc = s->d_sc;
   a.part = s->d_part;

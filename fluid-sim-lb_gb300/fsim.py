@@ -9,6 +9,7 @@ loading fails loudly when the library has not been built.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 import os
 from dataclasses import dataclass
 from pathlib import Path
@@ -106,6 +107,15 @@ _SIGS = {
     "fsim_reset_kernel_times": (C.c_int, [_P]),
     "fsim_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "fsim_cfl_noalloc": (C.c_int, [_P, _P, C.POINTER(C.c_int32), C.c_float, _P, _P]),
+    "fsim_rollout_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "fsim_rollout_destroy": (C.c_int, [_P]),
+    "fsim_rollout_particle_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "fsim_rollout_get_initial_velocity": (C.c_int, [_P, _P, _P]),
+    "fsim_rollout_set_initial_velocity": (C.c_int, [_P, _P, _P]),
+    "fsim_rollout_forward": (C.c_int, [_P, C.c_float, C.POINTER(fsim_pcg_params), _P,
+                                       C.POINTER(C.c_double)]),
+    "fsim_rollout_backward": (C.c_int, [_P, C.c_int32, C.POINTER(fsim_pcg_params), _P, _P]),
+    "fsim_rollout_replay_loss": (C.c_int, [_P, _P, _P, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -204,6 +214,7 @@ class Simulation:
         cfg.max_particles = max_particles
         cfg.device = device
         self.dims = tuple(int(x) for x in dims)
+        self._rollouts = weakref.WeakSet()  # closed before the handle
         h = C.c_void_p()
         rc = self.lib.fsim_create(C.byref(cfg), C.byref(h))
         if rc:
@@ -216,6 +227,8 @@ class Simulation:
             raise FsimError(rc, f"{what}: {self.lib.fsim_last_error(self.h).decode()}")
 
     def close(self):
+        for ro in list(getattr(self, "_rollouts", ())):
+            ro.close()
         if getattr(self, "h", None):
             self.lib.fsim_destroy(self.h)
             self.h = None
@@ -417,3 +430,109 @@ def physical_gravity(n: int) -> tuple[float, tuple]:
     """Gravity -9.8 with dx = 1/N in index space: 9.8*N cells/s^2."""
     g = float(np.float32(9.8 * n))
     return g, (0.0, g, 0.0)
+
+
+class Rollout:
+    """Differentiable rollout of a Simulation (fsim_rollout_*).
+
+    Captures the simulation's particle state as the initial state.  forward()
+    runs `steps` production steps at a fixed dt and returns the loss
+    0.5 * sum (u - target)^2 over the active in-box faces after the last step
+    (target: a dense face field as Simulation.field(FIELD_VELOCITY) returns);
+    backward() returns the gradients w.r.t. the initial particle velocity
+    and grid velocity ((n, 3) float64 each, initial particle order).
+    """
+
+    def __init__(self, sim: "Simulation", steps: int, checkpoint_every: int = 4):
+        self.sim = sim
+        self.lib = sim.lib
+        h = C.c_void_p()
+        sim._ck(self.lib.fsim_rollout_create(sim.h, steps, checkpoint_every, C.byref(h)),
+                "fsim_rollout_create")
+        self.h = h
+        sim._rollouts.add(self)
+        n = C.c_int64()
+        self.lib.fsim_rollout_particle_count(self.h, C.byref(n))
+        self.n = int(n.value)
+
+    def close(self):
+        # a rollout must be destroyed before its simulation's handle
+        if getattr(self, "h", None) and getattr(self.sim, "h", None):
+            self.lib.fsim_rollout_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _soa(a):
+        """(n, 3) -> contiguous SoA float64 (x | y | z)."""
+        return np.ascontiguousarray(np.asarray(a, dtype=np.float64).T)
+
+    def initial_velocity(self):
+        v = np.empty((3, self.n), np.float64)
+        g = np.empty((3, self.n), np.float64)
+        self.sim._ck(self.lib.fsim_rollout_get_initial_velocity(self.h, _ptr(v), _ptr(g)),
+                     "fsim_rollout_get_initial_velocity")
+        return v.T.copy(), g.T.copy()
+
+    def set_initial_velocity(self, vel, gvel=None):
+        v = self._soa(vel)
+        g = self._soa(vel if gvel is None else gvel)
+        self.sim._ck(self.lib.fsim_rollout_set_initial_velocity(self.h, _ptr(v), _ptr(g)),
+                     "fsim_rollout_set_initial_velocity")
+
+    def forward(self, dt: float, pcg: "fsim_pcg_params", target: np.ndarray) -> float:
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        loss = C.c_double()
+        self.sim._ck(self.lib.fsim_rollout_forward(self.h, C.c_float(dt), C.byref(pcg), _ptr(t),
+                                                   C.byref(loss)), "fsim_rollout_forward")
+        return float(loss.value)
+
+    def backward(self, adj: "fsim_pcg_params", tape: int = 0):
+        gv = np.empty((3, self.n), np.float64)
+        gg = np.empty((3, self.n), np.float64)
+        self.sim._ck(self.lib.fsim_rollout_backward(self.h, tape, C.byref(adj), _ptr(gv),
+                                                    _ptr(gg)), "fsim_rollout_backward")
+        return gv.T.copy(), gg.T.copy()
+
+    def replay_loss(self, vel=None, gvel=None) -> float:
+        v = None if vel is None else self._soa(vel)
+        g = None if gvel is None else self._soa(gvel)
+        loss = C.c_double()
+        self.sim._ck(self.lib.fsim_rollout_replay_loss(self.h, _ptr(v), _ptr(g), C.byref(loss)),
+                     "fsim_rollout_replay_loss")
+        return float(loss.value)
+
+
+def rollout_case(n: int, steps: int = 16, every: int = 4, dt: float = 1.0 / 300.0,
+                 sigma: float | None = None, noise_seed: int = 1, target_seed: int = 2,
+                 pcg: "fsim_pcg_params | None" = None, device: int = 0):
+    """The differentiable-rollout workload: the N^3 sphere drop (walls), 8
+    particles per cell from seed 0, initial velocities perturbed by Gaussian
+    noise sigma (index units; default 0.1 m/s with dx = 1/N, i.e. 0.1*N
+    cells/s) from noise_seed.  The target is the velocity field after the
+    same rollout with target_seed's noise.  Steps use a fixed dt and, unless
+    given, MIXED PCG to relative residual 1e-9.
+
+    Returns (sim, rollout, target, pcg)."""
+    g, f = physical_gravity(n)
+    sig = 0.1 * n if sigma is None else float(sigma)
+    if pcg is None:
+        pcg = pcg_params(PCG_RELATIVE, PREC_MIXED, 4000, tolerance=1e-9, inner_tolerance=1e-3,
+                         max_refinements=30)
+    t = Simulation((n, n, n), BOUNDARY_BOX, g, f, device=device)
+    t.seed(scene_passes("sphere_drop", n), seed=0)
+    t.perturb_velocities(sig, target_seed)
+    for _ in range(steps):
+        t.step(dt, pcg)
+    target, _ = t.field(FIELD_VELOCITY)
+    t.close()
+    sim = Simulation((n, n, n), BOUNDARY_BOX, g, f, device=device)
+    sim.seed(scene_passes("sphere_drop", n), seed=0)
+    sim.perturb_velocities(sig, noise_seed)
+    ro = Rollout(sim, steps, every)
+    return sim, ro, np.ascontiguousarray(target, dtype=np.float32), pcg

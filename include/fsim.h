@@ -264,6 +264,53 @@ int fsim_download_leaves(fsim_t* sim, int32_t* origins, int64_t capacity,
 int fsim_cfl_noalloc(const float* vel, const uint8_t* active, const int32_t dims[3],
                      float gravity, float* inv_speed, void* stream);
 
+/* ---- differentiable rollout (adjoint of projection and advection) ------ */
+/* No counterpart in the reference (the reference has no gradients).  A
+ * rollout of `steps` FLIP steps (the fsim_step sequence, box boundary) at a
+ * fixed dt from the particle state the handle holds at fsim_rollout_create,
+ * with the loss L = 0.5 * sum (u - u_target)^2 over the grid faces active
+ * after the last step's pressure update with their node in [0,N]^3; u_target
+ * is a dense face field in the layout of fsim_download_field.
+ *
+ * Gradients are those of the rollout with the discrete choices frozen at the
+ * forward run: particle binning and sort order, wall clamping and deletion,
+ * FLUID markers, active faces and the 1e-5 weight cut.  The pressure solves
+ * are taken as exact (A is symmetric, so the adjoint solve is the same PCG).
+ * The forward keeps a checkpoint of the particle state every
+ * checkpoint_every steps and the frozen topology of every step; the backward
+ * pass recomputes each segment from its checkpoint and reverses it.
+ * Adjoint values accumulate in fp64.  Particle arrays are SoA (x | y | z),
+ * 3*n doubles, in the order of the initial particle state. */
+typedef struct fsim_rollout fsim_rollout_t;
+/* A rollout borrows sim: destroy it before fsim_destroy(sim). */
+int fsim_rollout_create(fsim_t* sim, int32_t steps, int32_t checkpoint_every,
+                        fsim_rollout_t** out);
+int fsim_rollout_destroy(fsim_rollout_t* r);
+/* Number of particles of the initial state. */
+int fsim_rollout_particle_count(fsim_rollout_t* r, int64_t* n);
+/* Initial particle velocity (vel) and grid velocity (gvel), as doubles. */
+int fsim_rollout_get_initial_velocity(fsim_rollout_t* r, double* vel, double* gvel);
+/* Replaces the initial vel and gvel (rounded to float) before a forward. */
+int fsim_rollout_set_initial_velocity(fsim_rollout_t* r, const double* vel,
+                                      const double* gvel);
+/* The fp32 forward: fsim_step `steps` times (pcg: the solve parameters),
+ * recording checkpoints and topology; loss as above.  The handle is left
+ * holding the final state. */
+int fsim_rollout_forward(fsim_rollout_t* r, float dt, const fsim_pcg_params* pcg,
+                         const float* target, double* loss);
+/* Gradient of the loss w.r.t. the initial vel and gvel (either pointer may
+ * be null).  tape 0: linearised along the fp32 forward (recomputed from the
+ * checkpoints); tape 1: along an fp64 replay of the forward with the frozen
+ * topology (the fp64 reference gradient).  adj: parameters of the adjoint
+ * pressure solves (FP64 or MIXED precision; relative tolerance). */
+int fsim_rollout_backward(fsim_rollout_t* r, int32_t tape, const fsim_pcg_params* adj,
+                          double* grad_vel, double* grad_gvel);
+/* Loss of an fp64 replay of the forward with the frozen topology from the
+ * initial positions and the given initial vel / gvel (null: the stored
+ * ones); pressure solves in FP64 to relative residual 1e-12. */
+int fsim_rollout_replay_loss(fsim_rollout_t* r, const double* vel, const double* gvel,
+                             double* loss);
+
 /* ---- kernel timing (CUDA events on the handle's stream) --------------- */
 int fsim_set_profiling(fsim_t* sim, int32_t enabled);
 /* Accumulated per-kernel device time since the last reset.  Writes up to
