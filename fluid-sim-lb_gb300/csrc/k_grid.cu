@@ -96,6 +96,13 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
   __syncthreads();
   const float* px = a.part;
   const int64_t cap = a.cap;
+  // Each thread takes whole cells.  Per component D the particles of a cell
+  // reach an 18-node box (3 node positions on each tangential axis -- the
+  // stencil starts at the cell or one below it, by the side of the cell
+  // centre the particle is on -- and 2 on the normal axis); the thread sums
+  // the cell's particles into that box in registers, in list order, and
+  // flushes each node with one fixed-point atomic.  Trilinear weights are the
+  // products of the per-axis linear weights.
   for (int c = tid; c < 1000; c += 256) {
     const int ci = c / 100 - 1, cj = (c / 10) % 10 - 1, ck = c % 10 - 1;  // local [-1,8]
     const int ns = nb[nb_index(side(ci), side(cj), side(ck))];
@@ -103,49 +110,84 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
     const int g[3] = {org[0] + ci, org[1] + cj, org[2] + ck};
     const int vox = ((g[0] & 7) << 6) | ((g[1] & 7) << 3) | (g[2] & 7);
     const uint2 rg = a.cell_range[int64_t(ns) * 512 + vox];
-    for (uint32_t q = rg.x; q < rg.y; ++q) {
-      if (a.check_dead && a.keys[q] == kDeadKey) continue;
-      const float p[3] = {px[q], px[cap + q], px[2 * cap + q]};
-      const float u[3] = {px[3 * cap + q], px[4 * cap + q], px[5 * cap + q]};
+    if (rg.x >= rg.y) continue;
 #pragma unroll
-      for (int D = 0; D < 3; ++D) {
-        float lo[3] = {float(g[0]), float(g[1]), float(g[2])};
-        int st[3] = {g[0], g[1], g[2]};
+    for (int D = 0; D < 3; ++D) {
+      // box extents: 3 on the tangential axes, 2 on the normal axis D
+      constexpr int kE = 3;
+      const int e0 = D == 0 ? 2 : kE, e1 = D == 1 ? 2 : kE, e2 = D == 2 ? 2 : kE;
+      float am[18], aw[18];
+#pragma unroll
+      for (int t = 0; t < 18; ++t) { am[t] = 0.f; aw[t] = 0.f; }
+      unsigned reach = 0u;  // box nodes some particle's 8-node stencil includes
+      for (uint32_t q = rg.x; q < rg.y; ++q) {
+        if (a.check_dead && a.keys[q] == kDeadKey) continue;
+        const float uD = px[(3 + D) * cap + q];
+        float w1[3][3];   // per-axis weights over the box positions
+        unsigned m1[3];   // per-axis reached positions
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
-          if (ax == D) continue;
-          lo[ax] = __fadd_rn(lo[ax], 0.5f);
-          if (p[ax] < lo[ax]) { lo[ax] = __fsub_rn(lo[ax], 1.0f); st[ax] -= 1; }
-        }
-        const float x = __fsub_rn(p[0], lo[0]), y = __fsub_rn(p[1], lo[1]),
-                    z = __fsub_rn(p[2], lo[2]);
-        const float xy = __fmul_rn(x, y), yz = __fmul_rn(y, z), xz = __fmul_rn(z, x),
-                    xyz = __fmul_rn(xy, z);
-        float w[2][2][2];
-        w[1][1][1] = xyz;
-        w[1][1][0] = __fsub_rn(xy, xyz);
-        w[1][0][1] = __fsub_rn(xz, xyz);
-        w[1][0][0] = __fsub_rn(__fsub_rn(x, xz), w[1][1][0]);
-        w[0][1][1] = __fsub_rn(yz, xyz);
-        w[0][1][0] = __fsub_rn(__fsub_rn(y, yz), w[1][1][0]);
-        w[0][0][1] = __fsub_rn(__fsub_rn(z, yz), w[1][0][1]);
-        w[0][0][0] = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(1.0f, x), y), xy), w[0][0][1]);
-        const int l0 = st[0] - org[0], l1 = st[1] - org[1], l2 = st[2] - org[2];
-#pragma unroll
-        for (int di = 0; di < 2; ++di)
-#pragma unroll
-          for (int dj = 0; dj < 2; ++dj)
-#pragma unroll
-            for (int dk = 0; dk < 2; ++dk) {
-              const int i = l0 + di, j = l1 + dj, k = l2 + dk;
-              if ((unsigned)i < 8u && (unsigned)j < 8u && (unsigned)k < 8u) {
-                const int o = (i << 6) | (j << 3) | k;
-                const float ww = w[di][dj][dk];
-                atomicAdd(&sv[D][o], to_fix(__fmul_rn(ww, u[D])));
-                atomicAdd(&sw[D][o], to_fix(ww));
-                touched[o] = 1;
-              }
+          const float pa = px[ax * cap + q];
+          const float ga = float(g[ax]);
+          if (ax == D) {
+            const float x = __fsub_rn(pa, ga);
+            w1[ax][0] = __fsub_rn(1.0f, x); w1[ax][1] = x; w1[ax][2] = 0.f;
+            m1[ax] = 3u;
+          } else {
+            const float lo = __fadd_rn(ga, 0.5f);
+            if (pa < lo) {  // stencil starts one below the cell
+              const float f = __fsub_rn(pa, __fsub_rn(lo, 1.0f));
+              w1[ax][0] = __fsub_rn(1.0f, f); w1[ax][1] = f; w1[ax][2] = 0.f;
+              m1[ax] = 3u;
+            } else {
+              const float f = __fsub_rn(pa, lo);
+              w1[ax][0] = 0.f; w1[ax][1] = __fsub_rn(1.0f, f); w1[ax][2] = f;
+              m1[ax] = 6u;
             }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          if (i >= e0) continue;
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            if (j >= e1) continue;
+            const float wij = __fmul_rn(w1[0][i], w1[1][j]);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              if (k >= e2) continue;
+              const int t = (i * e1 + j) * e2 + k;
+              const float ww = __fmul_rn(wij, w1[2][k]);
+              am[t] = __fadd_rn(am[t], __fmul_rn(ww, uD));
+              aw[t] = __fadd_rn(aw[t], ww);
+              if (((m1[0] >> i) & (m1[1] >> j) & (m1[2] >> k)) & 1u) reach |= 1u << t;
+            }
+          }
+        }
+      }
+      // flush the box nodes that lie in this leaf
+      const int b0 = g[0] - (D == 0 ? 0 : 1) - org[0], b1 = g[1] - (D == 1 ? 0 : 1) - org[1],
+                b2 = g[2] - (D == 2 ? 0 : 1) - org[2];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        if (i >= e0) continue;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (j >= e1) continue;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            if (k >= e2) continue;
+            const int t = (i * e1 + j) * e2 + k;
+            const int li = b0 + i, lj = b1 + j, lk = b2 + k;
+            if (!((reach >> t) & 1u) || (unsigned)li >= 8u || (unsigned)lj >= 8u ||
+                (unsigned)lk >= 8u)
+              continue;
+            const int o = (li << 6) | (lj << 3) | lk;
+            atomicAdd(&sv[D][o], to_fix(am[t]));
+            atomicAdd(&sw[D][o], to_fix(aw[t]));
+            touched[o] = 1;
+          }
+        }
       }
     }
   }
@@ -156,8 +198,8 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
     const int g[3] = {org[0] + x, org[1] + y, org[2] + z};
     const bool on = touched[v] != 0;
     float val[3];
-#pragma unroll
     float wsum[3];
+#pragma unroll
     for (int D = 0; D < 3; ++D) {
       const float ws = from_fix(sw[D][v]);
       wsum[D] = ws;
