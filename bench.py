@@ -53,6 +53,10 @@ WORKLOADS = {
 #   pcg_update: read p_j, x, r (12) + flags (1); write x, r (8)       = 21 B
 ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update_mixed": 21,
              "pcg_spmv_f64": 25, "pcg_update_f64": 41}
+# DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
+# flushed before the launch) from one ncu capture of `bench.py --pcg-micro` on the 256^3
+# dam-break system (4.02 M unknowns); scaled by each step's unknowns.
+NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.80e6 / 4021250, "pcg_update": 61.39e6 / 4021250}
 
 
 def peaks():
@@ -256,6 +260,9 @@ def roofline(res):
     out = {"bound": "hbm", "kernel": name, "peak": peak, "peak_source": src, "unit": "GB/s",
            "share_of_step": tot_ms / res["prof_ms"] if res["prof_ms"] > 0 else None,
            "traffic": None}
+    if name in NCU_TRAFFIC_PER_UNKNOWN and res["prows"]:
+        out["traffic"] = NCU_TRAFFIC_PER_UNKNOWN[name] * float(np.mean(res["prows"]))
+        out["traffic_source"] = "ncu capture of the 256^3 system, scaled by unknowns"
     if name in ALG_BYTES and res["prows"]:
         alg = ALG_BYTES[name] * float(np.mean(res["prows"]))  # per working launch
         tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["prows"], res["piters"]))
