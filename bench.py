@@ -120,6 +120,25 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(values, device=None):
+    """Max of each value over the ranks of the default process group (the
+    slowest replica sets the whole-job time); identity without a group."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def whole_job_rate(world, steps, ms_max):
+    """Steps/s of the whole job: every replica runs `steps` steps; the job
+    takes the slowest replica's time."""
+    return world * steps / (ms_max * 1e-3)
+
+
 def pcg_cfg(args):
     import fsim
 
@@ -205,10 +224,6 @@ def run_gpu(args, rank, world):
     prof_ms = t1.elapsed_time(t2)
     kt = sim.kernel_times()
     sim.set_profiling(False)
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     n_fluid = float(np.mean(rows)) if rows else None
 
     # e2e: public API with host buffers (pinned), H2D + step + D2H per step
@@ -241,6 +256,7 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
     barrier()
+    ms, e2e_ms = max_over_ranks([ms, e2e_ms], device=f"cuda:{device}")
     sim.close()
     return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, clocks=clk.summary(),
                 piters=piters, prows=prows, prof_ms=prof_ms,
@@ -592,7 +608,7 @@ def main():
     res = run_gpu(args, rank, world)
     if rank != 0:
         return
-    value = world * args.steps / (res["ms"] * 1e-3)
+    value = whole_job_rate(world, args.steps, res["ms"])
     line = {"metric": "FLIP steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -600,7 +616,7 @@ def main():
                                                  fluid_cells=res["n_fluid"],
                                                  pcg_iters_per_step=float(np.mean(res["iters"]))),
             "roofline": roofline(res),
-            "e2e": {"value": 1e3 / res["e2e_ms"], "unit": "steps/s",
+            "e2e": {"value": whole_job_rate(world, 1, res["e2e_ms"]), "unit": "steps/s",
                     "h2d_bytes_per_step": res["e2e_bytes"], "d2h_bytes_per_step": res["e2e_bytes"]},
             "gpu_launches": res["launches"], "clocks": res["clocks"],
             "kernels_ms": {k: round(v[0], 3) for k, v in sorted(res["kt"].items(),
