@@ -188,6 +188,7 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         st = sim.step(next_dt(), prm)
         inv = st.next_inv_speed
+    free_b, total_b = torch.cuda.mem_get_info(device)  # after warm-up: all buffers exist
     launches0 = sim.launch_count()
     iters, rows = [], []
     barrier()
@@ -259,6 +260,7 @@ def run_gpu(args, rank, world):
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], device=f"cuda:{device}")
     sim.close()
     return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, clocks=clk.summary(),
+                device_memory_gb=(total_b - free_b) / 1e9,
                 piters=piters, prows=prows, prof_ms=prof_ms,
                 n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms,
                 e2e_bytes=36 * n_particles)
@@ -619,6 +621,7 @@ def main():
             "e2e": {"value": whole_job_rate(world, 1, res["e2e_ms"]), "unit": "steps/s",
                     "h2d_bytes_per_step": res["e2e_bytes"], "d2h_bytes_per_step": res["e2e_bytes"]},
             "gpu_launches": res["launches"], "clocks": res["clocks"],
+            "device_memory_gb": round(res["device_memory_gb"], 2),
             "kernels_ms": {k: round(v[0], 3) for k, v in sorted(res["kt"].items(),
                                                                 key=lambda kv: -kv[1][0])}}
     if not args.no_cpu:

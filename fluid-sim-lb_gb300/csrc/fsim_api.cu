@@ -248,6 +248,8 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
     s->use_graphs = g[0] != '0';
     s->use_pdl = g[0] == '2';
   }
+  // FSIM_PCG_COOP=1: the PCG iterations as one persistent cooperative kernel
+  if (const char* c = std::getenv("FSIM_PCG_COOP")) s->use_coop = c[0] == '1';
   for (int a = 0; a < 3; ++a) {
     s->lm.n[a] = cfg->global_dims[a];
     s->lm.lmax[a] = cfg->global_dims[a] / 8;

@@ -361,6 +361,21 @@ __device__ __forceinline__ void stcol(double* __restrict__ p, int64_t o, const C
   for (int k = 0; k < 4; ++k)
     *reinterpret_cast<double2*>(p + o + 2 * k) = make_double2(c.v[2 * k], c.v[2 * k + 1]);
 }
+// L2-only column load (data another CTA wrote earlier in the same launch)
+__device__ __forceinline__ void ldcol_cg(const float* p, int64_t o, Col<float>& c) {
+  const float4 a = __ldcg(reinterpret_cast<const float4*>(p + o));
+  const float4 b = __ldcg(reinterpret_cast<const float4*>(p + o + 4));
+  c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
+  c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
+}
+__device__ __forceinline__ void ldcol_cg(const double* p, int64_t o, Col<double>& c) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double2 a = __ldcg(reinterpret_cast<const double2*>(p + o + 2 * k));
+    c.v[2 * k] = a.x;
+    c.v[2 * k + 1] = a.y;
+  }
+}
 __device__ __forceinline__ uint2 ldflags(const uint8_t* __restrict__ f, int64_t o) {
   return ldv(reinterpret_cast<const uint2*>(f + o));
 }
@@ -775,6 +790,297 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   }
 }
 
+// ---- persistent PCG loop (cooperative launch) ------------------------------
+// All iterations in one launch: every CTA stays resident (cooperative launch)
+// and keeps its half leaves for the whole solve; the two grid-wide steps of
+// an iteration (p.Ap before alpha, r.r and r.z before beta) are a grid
+// barrier whose last-arriving CTA sums the per-CTA partials in a fixed order
+// (deterministic) and publishes the totals, so every CTA forms the same
+// alpha, beta and stop decision.  Loads of vectors other CTAs wrote in this
+// launch (halo columns, z-face planes) go to L2; a warp's own columns were
+// written by that warp, so they may use L1.  Each barrier wait is bounded:
+// past ~2^24 polls the CTA records FSIM_ERR_TIMEOUT and the solve ends.
+constexpr unsigned kBarrierPolls = 1u << 24;
+
+template <int DM, int NV>
+__device__ bool grid_reduce_sync(double (&v)[NV], double (&tot)[NV], const PcgArgs& a,
+                                 unsigned& gen) {
+  __shared__ int s_last, s_err;
+  __shared__ double s_res[NV];
+  block_sum<DM, NV, kHotThreads>(v);
+  PcgScalars* sc = a.sc;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a.part[k * a.maxb + blockIdx.x] = v[k];
+    __threadfence();
+    s_last = atomicAdd(&sc->bar_count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double* pk = a.part + k * a.maxb;
+      if (DM == 0) {
+        float x = 0.f;
+        for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += kHotThreads * 8) {
+          float t[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int i = i0 + u * kHotThreads;
+            t[u] = i < int(gridDim.x) ? float(__ldcg(pk + i)) : 0.f;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) x = __fadd_rn(x, t[u]);
+        }
+        acc[k] = double(x);
+      } else {
+        double x = 0.0;
+        for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += kHotThreads * 8) {
+          double t[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int i = i0 + u * kHotThreads;
+            t[u] = i < int(gridDim.x) ? __ldcg(pk + i) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) x += t[u];
+        }
+        acc[k] = x;
+      }
+    }
+    block_sum<DM, NV, kHotThreads>(acc);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        s_res[k] = acc[k];
+        sc->bar_tot[k] = acc[k];
+      }
+      sc->bar_count = 0u;
+      __threadfence();
+      atomicExch(&sc->bar_gen, gen + 1u);
+      s_err = __ldcg(&sc->bar_err) != 0u;
+    }
+  } else if (threadIdx.x == 0) {
+    volatile unsigned* g = &sc->bar_gen;
+    unsigned polls = 0;
+    while (*g == gen && polls < kBarrierPolls) {
+      __nanosleep(32);
+      ++polls;
+    }
+    const bool timed_out = *g == gen;
+    __threadfence();
+    if (timed_out) {
+      atomicExch(&sc->bar_err, 1u);
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) s_res[k] = __ldcg(&sc->bar_tot[k]);
+    }
+    s_err = timed_out || __ldcg(&sc->bar_err) != 0u;
+  }
+  __syncthreads();  // s_err is uniform across the CTA from here
+  ++gen;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = s_res[k];
+  return s_err == 0;
+}
+
+// p_j of the warp's half leaves, their p.Ap (one spmv phase)
+template <typename T, int DM>
+__device__ __forceinline__ void loop_spmv(const PcgArgs& a, Tile<T>& tile, const DiagInv<T>* tab,
+                                          int par, T beta, int hw0, int hstride, Dot<DM>& dp) {
+  const int lane = threadIdx.x & 31;
+  const T* r = static_cast<const T*>(a.r);
+  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
+  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
+  const int qold = 1 + (par ^ 1), qnew = 1 + par;
+  const T* zf = static_cast<const T*>(a.zf);
+  const int nhw = 2 * a.n_pleaf;
+  for (int hw = hw0; hw < nhw; hw += hstride) {
+    int fs[6];
+    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
+    const HalfLeaf h = half_pos(hw, lane);
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    const uint2 f = ldflags(a.flags, o);
+    Col<T> rc, pc, hr, hp;
+    ldcol(r, o, rc);
+    ldcol(pold, o, pc);
+    int hslot, hvox;
+    halo_col(h, fs, hslot, hvox);
+    const bool hv = hslot >= 0 && hslot < a.n_pleaf;
+    uint2 hf = make_uint2(0u, 0u);
+    if (hv) {
+      const int64_t hb = int64_t(hslot) * 512 + hvox;
+      hf = ldflags(a.flags, hb);
+      ldcol_cg(r, hb, hr);
+      ldcol_cg(pold, hb, hp);
+    } else {
+#pragma unroll
+      for (int z = 0; z < 8; ++z) hr.v[z] = hp.v[z] = T(0);
+    }
+    const int zs0 = fs[4], zs1 = fs[5];
+    const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+    const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + h.fidx;
+    const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + h.fidx;
+    const uint8_t zf0 = zv0 ? a.zff[int64_t(zs0) * 128 + 64 + h.fidx] : uint8_t(0);
+    const uint8_t zf1 = zv1 ? a.zff[int64_t(zs1) * 128 + h.fidx] : uint8_t(0);
+    const T zr0 = zv0 ? __ldcg(zf + zo0) : T(0), zr1 = zv1 ? __ldcg(zf + zo1) : T(0);
+    const T zq0 = zv0 ? __ldcg(zf + zo0 + 128 * qold) : T(0);
+    const T zq1 = zv1 ? __ldcg(zf + zo1 + 128 * qold) : T(0);
+    Col<T> P, H;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      P.v[z] = pnew_of<T>(tab, fbyte(f, z), rc.v[z], pc.v[z], beta);
+      H.v[z] = pnew_of<T>(tab, fbyte(hf, z), hr.v[z], hp.v[z], beta);
+    }
+    const T zm = pnew_of<T>(tab, zf0, zr0, zq0, beta);
+    const T zp = pnew_of<T>(tab, zf1, zr1, zq1, beta);
+    stcol(pnew, o, P);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
+      zw[0] = P.v[0];
+      zw[64] = P.v[7];
+    }
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, f, zm, zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
+  }
+}
+
+// x += alpha p, r -= alpha A p, r.r and r.z (one update phase)
+template <typename T, int DM>
+__device__ __forceinline__ void loop_update(const PcgArgs& a, Tile<T>& tile,
+                                            const DiagInv<T>* tab, int par, T alpha, int hw0,
+                                            int hstride, Dot<DM>& drr, Dot<DM>& drz) {
+  const int lane = threadIdx.x & 31;
+  const T* p = static_cast<const T*>(par ? a.p1 : a.p0);
+  T* x = static_cast<T*>(a.x);
+  T* r = static_cast<T*>(a.r);
+  const int qcur = 1 + par;
+  const T nalpha = -alpha;
+  const int nhw = 2 * a.n_pleaf;
+  for (int hw = hw0; hw < nhw; hw += hstride) {
+    int fs[6];
+    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
+    const HalfLeaf h = half_pos(hw, lane);
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    const uint2 f = ldflags(a.flags, o);
+    Col<T> P, H, xc, rc;
+    ldcol(p, o, P);
+    ldcol(x, o, xc);
+    ldcol(r, o, rc);
+    int hslot, hvox;
+    halo_col(h, fs, hslot, hvox);
+    if (hslot >= 0 && hslot < a.n_pleaf) {
+      ldcol_cg(p, int64_t(hslot) * 512 + hvox, H);
+    } else {
+#pragma unroll
+      for (int z = 0; z < 8; ++z) H.v[z] = T(0);
+    }
+    const int zs0 = fs[4], zs1 = fs[5];
+    const T* zfp = static_cast<const T*>(a.zf) + 128 * qcur + h.fidx;
+    const T zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? __ldcg(zfp + int64_t(zs0) * 384 + 64) : T(0);
+    const T zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? __ldcg(zfp + int64_t(zs1) * 384) : T(0);
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, f, zm, zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      const uint8_t g = fbyte(f, z);
+      xc.v[z] = tadd(tmul(alpha, P.v[z]), xc.v[z]);
+      rc.v[z] = tadd(tmul(nalpha, ap.v[z]), rc.v[z]);
+      drr.add(rc.v[z], rc.v[z]);
+      drz.add(rc.v[z], tmul(tab[g & 15].inv, rc.v[z]));
+    }
+    stcol(x, o, xc);
+    stcol(r, o, rc);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + h.fidx;
+      zw[0] = rc.v[0];
+      zw[64] = rc.v[7];
+    }
+  }
+}
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
+    k_pcg_loop(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  __shared__ unsigned s_gen;
+  PcgScalars* sc = a.sc;
+  fill_diag_table<T>(tab);
+  if (threadIdx.x == 0) s_gen = *reinterpret_cast<volatile unsigned*>(&sc->bar_gen);
+  __syncthreads();
+  unsigned gen = s_gen;
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
+  const int wpb = kHotThreads / 32;
+  const int hw0 = blockIdx.x * wpb + (threadIdx.x >> 5), hstride = gridDim.x * wpb;
+  const bool fp32 = sc->fp32 != 0;
+  int it = sc->iter, done = sc->done, status = sc->status;
+  const int max_iter = sc->max_iter;
+  double rz = sc->rz, rr = sc->rr, beta = sc->beta, alpha = 0.0, pAp = 0.0, rz_old = sc->rz_old;
+  bool ok = true;
+  while (!done) {
+    const int par = it & 1;
+    {
+      Dot<DM> dp;
+      loop_spmv<T, DM>(a, tile, tab, par, T(beta), hw0, hstride, dp);
+      double v[1] = {dp.value()}, tot[1];
+      if (!(ok = grid_reduce_sync<DM, 1>(v, tot, a, gen))) break;
+      pAp = fp32 ? double(float(tot[0])) : tot[0];
+      alpha = fp32 ? double(__fdiv_rn(float(rz), float(pAp))) : rz / pAp;
+      if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
+        status = FSIM_ERR_BREAKDOWN;
+        done = 1;
+        break;
+      }
+    }
+    {
+      Dot<DM> drr, drz;
+      loop_update<T, DM>(a, tile, tab, par, T(alpha), hw0, hstride, drr, drz);
+      double v[2] = {drr.value(), drz.value()}, tot[2];
+      if (!(ok = grid_reduce_sync<DM, 2>(v, tot, a, gen))) break;
+      rr = fp32 ? double(float(tot[0])) : tot[0];
+      rz_old = rz;
+      rz = fp32 ? double(float(tot[1])) : tot[1];
+      beta = fp32 ? double(__fdiv_rn(float(rz), float(rz_old))) : rz / rz_old;
+      ++it;
+      if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
+        status = FSIM_ERR_BREAKDOWN;
+        done = 1;
+      } else {
+        done = (it >= max_iter) || converged(sc, rr);
+      }
+    }
+  }
+  if (!ok) {
+    status = FSIM_ERR_TIMEOUT;
+    done = 1;
+  }
+  // every CTA holds the same scalars; one writes them back
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->iter = it;
+    sc->done = done;
+    sc->status = status;
+    sc->rr = rr;
+    sc->rz = rz;
+    sc->rz_old = rz_old;
+    sc->alpha = alpha;
+    sc->beta = beta;
+    sc->pAp = pAp;
+  }
+}
+
 // MIXED: x64 += d (inner solution); d is the fp32 x of the inner solve.
 __global__ void k_accumulate_x64(const __grid_constant__ PcgArgs a) {
   const int64_t n = int64_t(a.n_pleaf) * 512;
@@ -907,6 +1213,33 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks}));
+  if (s->use_coop && !s->profiling) {
+    // one cooperative launch runs every iteration (setup has already run)
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_loop<T, DM>, kHotThreads, 0);
+    const int cgrid = std::min({std::max(occ, 0) * s->num_sms, (2 * a.n_pleaf + wpb - 1) / wpb,
+                                s->max_blocks});
+    if (cgrid > 0) {
+      PcgArgs ca = a;
+      ca.cond = 0;
+      void* args[] = {&ca};
+      ProfScope ps(s, nm_spmv);
+      cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_pcg_loop<T, DM>),
+                                                  dim3(unsigned(cgrid)), dim3(kHotThreads), args,
+                                                  0, s->stream);
+      if (e == cudaSuccess) {
+        s->launches += 1;
+        FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                   s->stream));
+        FSIM_CK(s, cudaStreamSynchronize(s->stream));
+        if (s->h_sc->status == FSIM_ERR_TIMEOUT)
+          return fail(s, FSIM_ERR_TIMEOUT, "PCG grid barrier timed out");
+        return FSIM_OK;
+      }
+      cudaGetLastError();  // refused (e.g. not co-resident): use the graph loop
+      s->use_coop = false;
+    }
+  }
   if (s->use_graphs && !s->profiling) {
     int rc = FSIM_ERR_CUDA;
     if (s->use_pdl) {
