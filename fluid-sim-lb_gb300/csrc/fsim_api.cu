@@ -250,6 +250,8 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   }
   // FSIM_PCG_COOP=1: the PCG iterations as one persistent cooperative kernel
   if (const char* c = std::getenv("FSIM_PCG_COOP")) s->use_coop = c[0] == '1';
+  // FSIM_PCG_PIPE=0: the unpipelined hot kernels
+  if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
   for (int a = 0; a < 3; ++a) {
     s->lm.n[a] = cfg->global_dims[a];
     s->lm.lmax[a] = cfg->global_dims[a] / 8;

@@ -790,6 +790,253 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   }
 }
 
+// ---- register-pipelined variants --------------------------------------------
+// The same two kernels with every input of the next half leaf (own column,
+// halo column, z faces) loaded into registers while the current half leaf
+// computes: each warp keeps one half leaf of loads in flight, at the price of
+// about 40 more registers (4 CTAs per SM instead of 6).
+template <typename T>
+struct SpmvIn {
+  uint2 f, hf;
+  Col<T> rc, pc, hr, hp;
+  uint8_t zf0, zf1;
+  T zr0, zr1, zq0, zq1;
+};
+
+template <typename T>
+__device__ __forceinline__ void spmv_load(const PcgArgs& a, int hw, int lane, const int fs[6],
+                                          const T* r, const T* pold, int qold, SpmvIn<T>& in) {
+  const HalfLeaf h = half_pos(hw, lane);
+  const int64_t o = int64_t(h.s) * 512 + h.c;
+  in.f = ldflags(a.flags, o);
+  ldcol(r, o, in.rc);
+  ldcol(pold, o, in.pc);
+  int hslot, hvox;
+  halo_col(h, fs, hslot, hvox);
+  const bool hv = hslot >= 0 && hslot < a.n_pleaf;
+  const int64_t hb = int64_t(hv ? hslot : 0) * 512 + hvox;
+  in.hf = make_uint2(0u, 0u);
+  if (hv) {
+    in.hf = ldflags(a.flags, hb);
+    ldcol(r, hb, in.hr);
+    ldcol(pold, hb, in.hp);
+  } else {
+#pragma unroll
+    for (int z = 0; z < 8; ++z) in.hr.v[z] = in.hp.v[z] = T(0);
+  }
+  const int zs0 = fs[4], zs1 = fs[5];
+  const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+  const T* zf = static_cast<const T*>(a.zf);
+  const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + h.fidx;
+  const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + h.fidx;
+  in.zf0 = zv0 ? ldv(a.zff + int64_t(zs0) * 128 + 64 + h.fidx) : uint8_t(0);
+  in.zf1 = zv1 ? ldv(a.zff + int64_t(zs1) * 128 + h.fidx) : uint8_t(0);
+  in.zr0 = zv0 ? ldv(zf + zo0) : T(0);
+  in.zr1 = zv1 ? ldv(zf + zo1) : T(0);
+  in.zq0 = zv0 ? ldv(zf + zo0 + 128 * qold) : T(0);
+  in.zq1 = zv1 ? ldv(zf + zo1 + 128 * qold) : T(0);
+}
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  const int par = a.par;
+  const T* r = static_cast<const T*>(a.r);
+  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
+  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
+  const int qold = 1 + (par ^ 1), qnew = 1 + par;
+  const int lane = threadIdx.x & 31;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  fill_diag_table<T>(tab);
+  const PcgScalars* sc = a.sc;
+  const int done = sc->done;
+  const T beta = T(sc->beta);
+  SpmvIn<T> cur;
+  int nbl = -1;
+  if (hw < nhw) {
+    int fs[6];
+    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
+    spmv_load<T>(a, hw, lane, fs, r, pold, qold, cur);
+    nbl = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+  }
+  __syncthreads();
+  if (done) return;
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
+  Dot<DM> dp;
+  while (hw < nhw) {
+    const int hn = hw + hstride;
+    SpmvIn<T> nxt;
+    if (hn < nhw) {
+      int fs[6];
+      face_slots(nbl, fs);
+      spmv_load<T>(a, hn, lane, fs, r, pold, qold, nxt);
+      nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
+    }
+    const HalfLeaf h = half_pos(hw, lane);
+    Col<T> P, H;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      P.v[z] = pnew_of<T>(tab, fbyte(cur.f, z), cur.rc.v[z], cur.pc.v[z], beta);
+      H.v[z] = pnew_of<T>(tab, fbyte(cur.hf, z), cur.hr.v[z], cur.hp.v[z], beta);
+    }
+    const T zm = pnew_of<T>(tab, cur.zf0, cur.zr0, cur.zq0, beta);
+    const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    stcol(pnew, o, P);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
+      zw[0] = P.v[0];
+      zw[64] = P.v[7];
+    }
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, cur.f, zm, zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
+    cur = nxt;
+    hw = hn;
+  }
+  double v[1] = {dp.value()};
+  double tot[1];
+  if (grid_sum<DM, 1, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
+    PcgScalars* s = a.sc;
+    s->pAp = round_t(s, tot[0]);
+    double alpha = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->pAp))) : s->rz / s->pAp;
+    s->alpha = alpha;
+    if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
+      s->status = FSIM_ERR_BREAKDOWN;
+      s->done = 1;
+    }
+  }
+}
+
+template <typename T>
+struct UpdIn {
+  uint2 f;
+  Col<T> P, x, r, H;
+  T zm, zp;
+};
+
+template <typename T>
+__device__ __forceinline__ void upd_load(const PcgArgs& a, int hw, int lane, const int fs[6],
+                                         const T* p, const T* x, const T* r, int qcur,
+                                         UpdIn<T>& in) {
+  const HalfLeaf h = half_pos(hw, lane);
+  const int64_t o = int64_t(h.s) * 512 + h.c;
+  in.f = ldflags(a.flags, o);
+  ldcol(p, o, in.P);
+  ldcol(x, o, in.x);
+  ldcol(r, o, in.r);
+  int hslot, hvox;
+  halo_col(h, fs, hslot, hvox);
+  if (hslot >= 0 && hslot < a.n_pleaf) {
+    ldcol(p, int64_t(hslot) * 512 + hvox, in.H);
+  } else {
+#pragma unroll
+    for (int z = 0; z < 8; ++z) in.H.v[z] = T(0);
+  }
+  const int zs0 = fs[4], zs1 = fs[5];
+  const T* zfp = static_cast<const T*>(a.zf) + 128 * qcur + h.fidx;
+  in.zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? ldv(zfp + int64_t(zs0) * 384 + 64) : T(0);
+  in.zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + int64_t(zs1) * 384) : T(0);
+}
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kHotThreads, 4)
+    k_pcg_update_pl(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  const int par = a.par;
+  const T* p = static_cast<const T*>(par ? a.p1 : a.p0);
+  T* x = static_cast<T*>(a.x);
+  T* r = static_cast<T*>(a.r);
+  const int qcur = 1 + par;
+  const int lane = threadIdx.x & 31;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  fill_diag_table<T>(tab);
+  const PcgScalars* sc = a.sc;
+  const int done = sc->done;
+  const int it = sc->iter;
+  const T alpha = T(sc->alpha);
+  UpdIn<T> cur;
+  int nbl = -1;
+  if (hw < nhw) {
+    int fs[6];
+    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
+    upd_load<T>(a, hw, lane, fs, p, x, r, qcur, cur);
+    nbl = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+  }
+  __syncthreads();
+  if (done) {
+    if (a.cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
+    return;
+  }
+  const T nalpha = -alpha;
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
+  Dot<DM> drr, drz;
+  while (hw < nhw) {
+    const int hn = hw + hstride;
+    UpdIn<T> nxt;
+    if (hn < nhw) {
+      int fs[6];
+      face_slots(nbl, fs);
+      upd_load<T>(a, hn, lane, fs, p, x, r, qcur, nxt);
+      nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
+    }
+    const HalfLeaf h = half_pos(hw, lane);
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, cur.P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, cur.H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, cur.P, cur.f, cur.zm, cur.zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      const uint8_t g = fbyte(cur.f, z);
+      cur.x.v[z] = tadd(tmul(alpha, cur.P.v[z]), cur.x.v[z]);
+      cur.r.v[z] = tadd(tmul(nalpha, ap.v[z]), cur.r.v[z]);
+      drr.add(cur.r.v[z], cur.r.v[z]);
+      drz.add(cur.r.v[z], tmul(tab[g & 15].inv, cur.r.v[z]));
+    }
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    stcol(x, o, cur.x);
+    stcol(r, o, cur.r);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + h.fidx;
+      zw[0] = cur.r.v[0];
+      zw[64] = cur.r.v[7];
+    }
+    cur = nxt;
+    hw = hn;
+  }
+  double v[2] = {drr.value(), drz.value()};
+  double tot[2];
+  if (grid_sum<DM, 2, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
+    PcgScalars* s = a.sc;
+    s->rr = round_t(s, tot[0]);
+    s->rz_old = s->rz;
+    s->rz = round_t(s, tot[1]);
+    double beta = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->rz_old))) : s->rz / s->rz_old;
+    s->beta = beta;
+    s->iter = it + 1;
+    if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
+      s->status = FSIM_ERR_BREAKDOWN;
+      s->done = 1;
+    } else {
+      s->done = (s->iter >= s->max_iter) || converged(s, s->rr);
+    }
+    if (a.cond) cudaGraphSetConditional(a.cond, s->done ? 0u : 1u);
+  }
+}
+
 // ---- persistent PCG loop (cooperative launch) ------------------------------
 // All iterations in one launch: every CTA stays resident (cooperative launch)
 // and keeps its half leaves for the whole solve; the two grid-wide steps of
@@ -1169,8 +1416,12 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl) {
       kn.kernel.gridDim = dim3(unsigned(wgrid));
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
-      kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
-                               : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+      if ((s->use_pipe && sizeof(T) == 4))
+        kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update_pl<T, DM>)
+                                 : reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM>);
+      else
+        kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
+                                 : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
       cudaGraphEdgeData ed = {};
       if (pdl) {
         ed.from_port = cudaGraphKernelNodePortProgrammatic;
@@ -1208,8 +1459,13 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
   const int wpb = kHotThreads / 32;
   int occ_a = 1, occ_b = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_pcg_spmv<T, DM>, kHotThreads, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_pcg_update<T, DM>, kHotThreads, 0);
+  if ((s->use_pipe && sizeof(T) == 4)) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_pcg_spmv_pl<T, DM>, kHotThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_pcg_update_pl<T, DM>, kHotThreads, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_pcg_spmv<T, DM>, kHotThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_pcg_update<T, DM>, kHotThreads, 0);
+  }
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks}));
@@ -1269,8 +1525,13 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     if (s->h_sc->done) break;
     for (int c = 0; c < chunk; ++c, ++launched) {
       a.par = int(launched & 1);
-      FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kHotThreads, 0, a);
-      FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kHotThreads, 0, a);
+      if ((s->use_pipe && sizeof(T) == 4)) {
+        FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv_pl<T, DM>), wgrid, kHotThreads, 0, a);
+        FSIM_LAUNCH(s, nm_upd, (k_pcg_update_pl<T, DM>), wgrid, kHotThreads, 0, a);
+      } else {
+        FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kHotThreads, 0, a);
+        FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kHotThreads, 0, a);
+      }
     }
     if (chunk < 64) chunk *= 2;
   }
