@@ -173,6 +173,8 @@ int after_sort(fsim_sim* s) {
 
 }  // namespace
 
+int grow_particle_capacity(fsim_sim* s, int64_t n) { return ensure_particle_capacity(s, n); }
+
 int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf) {
   int rc;
   if (n_gleaf > s->cap_leaf) {
@@ -219,7 +221,7 @@ extern "C" {
 const char* fsim_version(void) { return "fsim-gb300 0.1 (sm_103a)"; }
 
 const char* fsim_last_error(const fsim_t* sim) {
-  if (!sim) return "null handle";
+  if (!sim) return g_scene_err.empty() ? "null handle" : g_scene_err.c_str();
   return sim->err.c_str();
 }
 
@@ -293,7 +295,8 @@ int fsim_destroy(fsim_t* s) {
   if (s->dev >= 0) cudaSetDevice(s->dev);
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (int b = 0; b < 2; ++b) { dfree(s->part[b]); dfree(s->keys[b]); dfree(s->vals[b]); }
-  dfree(s->sort_tmp); dfree(s->scan_tmp);
+  dfree(s->sort_tmp); dfree(s->scan_tmp); dfree(s->keys64[0]); dfree(s->keys64[1]);
+  if (s->src_tmp) cudaFree(s->src_tmp);
   dfree(s->d_flag); dfree(s->d_slot); dfree(s->d_scan); dfree(s->d_leaf_id); dfree(s->d_nbr);
   dfree(s->d_cell_range); dfree(s->d_leaf_range);
   dfree(s->vel); dfree(s->vold); dfree(s->weight); dfree(s->vel_on); dfree(s->vold_on);
@@ -338,14 +341,11 @@ int fsim_add_solid_cuboid(fsim_t* s, const int32_t lo[3], const int32_t hi[3]) {
 int fsim_seed_fluid(fsim_t* s, const fsim_seed_pass* passes, int32_t npasses, uint64_t seed) {
   if (!s || (npasses > 0 && !passes)) return FSIM_ERR_INVALID;
   cudaSetDevice(s->dev);
-  // upper bound for capacity: (passes * nppc) per cell is too loose; the
-  // count sweep inside seed_fluid gives the exact number
-  int64_t ncell = int64_t(s->lm.n[0]) * s->lm.n[1] * s->lm.n[2];
-  (void)ncell;
   // count first with the current capacity; seed_fluid fails with CAPACITY
   // when it does not fit, then grow and retry once.
   s->n_total = 0;
   s->n_live = 0;
+  s->seed = seed;
   int rc = seed_fluid(s, passes, npasses, seed);
   if (rc == FSIM_ERR_CAPACITY) {
     const int64_t need = s->h_cnt[5];
@@ -354,6 +354,47 @@ int fsim_seed_fluid(fsim_t* s, const fsim_seed_pass* passes, int32_t npasses, ui
   }
   if (rc) return rc;
   return after_sort(s);
+}
+
+int fsim_add_source(fsim_t* s, const fsim_source* src) {
+  if (!s || !src) return FSIM_ERR_INVALID;
+  if (s->sources.size() >= size_t(FSIM_MAX_SOURCES))
+    return fail(s, FSIM_ERR_CAPACITY, "at most FSIM_MAX_SOURCES sources");
+  if (src->velocity_oscillating && !(src->box_period != 0.f))
+    return fail(s, FSIM_ERR_INVALID, "an oscillating velocity needs box_period != 0");
+  s->sources.push_back(*src);
+  return FSIM_OK;
+}
+
+int fsim_set_time(fsim_t* s, double t) {
+  if (!s) return FSIM_ERR_INVALID;
+  s->time = t;
+  return FSIM_OK;
+}
+
+int fsim_get_time(fsim_t* s, double* t) {
+  if (!s || !t) return FSIM_ERR_INVALID;
+  *t = s->time;
+  return FSIM_OK;
+}
+
+int fsim_add_contribution_from_sources(fsim_t* s, float t) {
+  if (!s) return FSIM_ERR_INVALID;
+  cudaSetDevice(s->dev);
+  int rc = need_topology(s);
+  if (rc) return rc;
+  return add_source_particles(s, t);
+}
+
+int fsim_delete_fluid_in_sources(fsim_t* s, float t) {
+  if (!s) return FSIM_ERR_INVALID;
+  cudaSetDevice(s->dev);
+  int rc = need_topology(s);
+  if (rc) return rc;
+  if (s->sources.empty()) return FSIM_OK;
+  if ((rc = delete_in_sources(s, t))) return rc;
+  s->deleted_outside = true;  // dead keys among the live ones until the next sort
+  return FSIM_OK;
 }
 
 int fsim_perturb_velocities(fsim_t* s, float sigma, uint64_t seed) {
@@ -601,6 +642,14 @@ int fsim_step(fsim_t* s, float dt, const fsim_pcg_params* prm, fsim_step_stats* 
   if (!s || !prm) return FSIM_ERR_INVALID;
   int rc = need_topology(s);
   if (rc) return rc;
+  const float t = float(s->time);  // advanced_time_ (T = float)
+  if (!s->sources.empty()) {
+    // AddContributionFromSources(t); DeleteFluidInSources(t) is applied by
+    // the advection kernel right after the move
+    if ((rc = add_source_particles(s, t))) return rc;
+    s->delete_in_sources = true;
+    s->src_time = t;
+  }
   // MoveParticles + DeleteParticlesInSolids
   if ((rc = launch_keys_from_positions(s, 1, dt))) return rc;
   if ((rc = rebuild_topology(s))) return rc;
@@ -634,6 +683,7 @@ int fsim_step(fsim_t* s, float dt, const fsim_pcg_params* prm, fsim_step_stats* 
     st->pcg = ps;
     st->next_inv_speed = inv_speed_from(s, vmax);
   }
+  s->time = double(t + dt);  // AdvanceTime, in T = float
   if (ps.status == FSIM_ERR_BREAKDOWN)
     return fail(s, FSIM_ERR_BREAKDOWN, "PCG breakdown: alpha or beta exceeded 1e5");
   return FSIM_OK;

@@ -264,6 +264,22 @@ struct fsim_sim {
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;
 
+  // water sources and the time they see
+  std::vector<fsim_source> sources;
+  double time = 0.0;
+  uint64_t seed = 0;         // of the last seeding (source draws use it)
+  int64_t source_calls = 0;  // AddContributionFromSources calls (draw stream)
+  // the next sort orders by (new key, old key): particles were appended
+  // after the sorted array (source particles)
+  bool composite_sort = false;
+  // regions whose particles the next advection deletes (DeleteFluidInSources)
+  bool delete_in_sources = false;
+  float src_time = 0.f;
+  uint64_t* keys64[2] = {nullptr, nullptr};
+  int64_t cap64 = 0;
+  void* src_tmp = nullptr;   // source draw counts and offsets
+  size_t src_tmp_bytes = 0;
+
   // profiling
   bool profiling = false;
   std::vector<fsim::KernelStat> kstats;
@@ -281,6 +297,7 @@ struct fsim_sim {
 namespace fsim {
 
 int fail(fsim_sim* s, int code, const std::string& msg);
+extern thread_local std::string g_scene_err;  // last fsim_scene_parse error
 int cuda_fail(fsim_sim* s, cudaError_t e, const char* what);
 
 struct ProfScope {
@@ -292,7 +309,10 @@ struct ProfScope {
 };
 
 int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf);
+// particle arrays for at least n particles (the current ones are kept)
+int grow_particle_capacity(fsim_sim* s, int64_t n);
 int rebuild_topology(fsim_sim* s);  // from keys[cur]/vals, n_total
+int rebuild_after_sort(fsim_sim* s);  // the topology part, keys[0]/vals[0] sorted
 
 // kernel entry points implemented in the .cu files
 int launch_keys_from_positions(fsim_sim* s, int mode, float dt);
@@ -313,6 +333,14 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st,
 int download_dense(fsim_sim* s, int field, float* out, uint8_t* active);
 int download_marker(fsim_sim* s, int32_t* out, uint8_t* active);
 int seed_fluid(fsim_sim* s, const fsim_seed_pass* passes, int npasses, uint64_t seed);
+// AddContributionFromSources(t): appends the active sources' particles
+int add_source_particles(fsim_sim* s, float t);
+// DeleteFluidInSources(t) on the current (sorted) particles: dead keys
+int delete_in_sources(fsim_sim* s, float t);
+// get_box(t) / get_velocity(t) / is_active(t) of Source<T> (host)
+void source_box(const fsim_source& src, float t, float lo[3], float hi[3]);
+void source_velocity(const fsim_source& src, float t, float v[3]);
+bool source_active(const fsim_source& src, float t);
 int perturb(fsim_sim* s, float sigma, uint64_t seed);
 
 }  // namespace fsim

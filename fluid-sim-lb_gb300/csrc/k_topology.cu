@@ -9,6 +9,10 @@
 // particles in visiting order); a gather of the 9 particle arrays; and the
 // leaf topology (particle leaves, one-leaf dilation, slots, 27-neighbour
 // table, per-cell particle ranges).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
@@ -16,7 +20,44 @@
 
 namespace fsim {
 
+// ---- Source<T> (common/sources.cc:66-109), evaluated on the host --------
+void source_box(const fsim_source& src, float t, float lo[3], float hi[3]) {
+  (void)t;  // the oscillating branch of get_box assigns a shadowed local
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = src.lo[d];
+    hi[d] = src.hi[d] - 1.0f;  // box.set_end(box.get_end() - Vec3(1))
+  }
+}
+void source_velocity(const fsim_source& src, float t, float v[3]) {
+  if (!src.velocity_oscillating) {
+    for (int d = 0; d < 3; ++d) v[d] = src.velocity[d];
+    return;
+  }
+  const float w = float(M_PI * double(t) / double(src.box_period));  // T w = M_PI*t/box_period_
+  for (int d = 0; d < 3; ++d)
+    v[d] = float(double(src.velocity[d]) +
+                 0.5 * double(src.velocity2[d] - src.velocity[d]) * (double(std::cos(w)) + 1.0));
+}
+bool source_active(const fsim_source& src, float t) {
+  return !src.timed || (t >= src.start_time && t <= src.end_time);
+}
+
 namespace {
+
+// Boxes of DeleteFluidInSources (get_box(t) of every source), passed by value.
+struct SourceRegions {
+  int n;
+  float lo[FSIM_MAX_SOURCES][3], hi[FSIM_MAX_SOURCES][3];
+};
+__device__ __forceinline__ bool in_regions(const SourceRegions& r, const float p[3]) {
+  for (int q = 0; q < r.n; ++q) {
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) in &= (p[d] >= r.lo[q][d]) & (p[d] <= r.hi[q][d]);  // Cube::IsInside
+    if (in) return true;
+  }
+  return false;
+}
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
@@ -24,10 +65,16 @@ __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b)
 // mode 0: key from current position (upload); positions outside [0,N]
 //         are counted as invalid.
 // mode 1: advect by gvel*dt, clamp, delete in solids (MoveParticles).
+// mode 1 extras: particles inside a source region get the dead key
+// (DeleteFluidInSources right after MoveParticles); kout64 (optional) gets
+// (new key << 32 | old key), so that a stable sort on it orders particles as
+// the reference's rebuilt lists do when particles were appended to cell lists
+// (the visiting order is by old cell, then list position).
 __global__ void k_keys(float* __restrict__ part, int64_t cap, const uint32_t* __restrict__ kcur,
                        uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
                        LeafMap lm, SolidDesc sd, int mode, float dt,
-                       unsigned long long* __restrict__ invalid) {
+                       unsigned long long* __restrict__ invalid, const SourceRegions reg,
+                       unsigned long long* __restrict__ kout64) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   vout[i] = uint32_t(i);
@@ -37,6 +84,7 @@ __global__ void k_keys(float* __restrict__ part, int64_t cap, const uint32_t* __
   if (mode == 1) {
     if (kcur[i] == kDeadKey) {
       kout[i] = kDeadKey;
+      if (kout64) kout64[i] = ~0ull;
       return;
     }
     const float g[3] = {gx[i], gx[cap + i], gx[2 * cap + i]};
@@ -55,7 +103,11 @@ __global__ void k_keys(float* __restrict__ part, int64_t cap, const uint32_t* __
     px[i] = p[0];
     px[cap + i] = p[1];
     px[2 * cap + i] = p[2];
-    kout[i] = is_solid(sd, id[0], id[1], id[2]) ? kDeadKey : cell_key(lm, id[0], id[1], id[2]);
+    uint32_t k = is_solid(sd, id[0], id[1], id[2]) ? kDeadKey : cell_key(lm, id[0], id[1], id[2]);
+    if (reg.n > 0 && in_regions(reg, p)) k = kDeadKey;
+    kout[i] = k;
+    if (kout64)
+      kout64[i] = (k == kDeadKey) ? ~0ull : ((static_cast<unsigned long long>(k) << 32) | kcur[i]);
   } else {
     bool ok = true;
     int id[3];
@@ -306,16 +358,117 @@ __global__ void k_perturb(float* __restrict__ part, int64_t cap, int64_t n, floa
   }
 }
 
+// ---- AddContributionFromSources (common/flip_simulation.cc:1207-1270) ----
+// Work items are (source, cell) pairs, sources in order and each source's
+// cells x-major, so that particles land in the reference's list order after
+// an exclusive scan of the per-item counts.
+struct SourceGen {
+  int nsrc;
+  int lo[FSIM_MAX_SOURCES][3], dim[FSIM_MAX_SOURCES][3];  // cell range of each source
+  int64_t begin[FSIM_MAX_SOURCES + 1];                    // first work item of each source
+  float blo[FSIM_MAX_SOURCES][3], bhi[FSIM_MAX_SOURCES][3];  // get_box(t)
+  float vel[FSIM_MAX_SOURCES][3];
+  int pass[FSIM_MAX_SOURCES];
+  uint64_t seed;
+  int nppc;
+};
+
+// count == nullptr: write pass (offsets from the scan)
+__global__ void k_source(const __grid_constant__ SourceGen g, LeafMap lm, uint32_t* __restrict__ cnt,
+                         const uint32_t* __restrict__ off, float* __restrict__ part, int64_t cap,
+                         int64_t base, uint32_t* __restrict__ kout) {
+  const int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= g.begin[g.nsrc]) return;
+  int q = 0;
+  while (w >= g.begin[q + 1]) ++q;
+  const int64_t c = w - g.begin[q];
+  const int dy = g.dim[q][1], dz = g.dim[q][2];
+  const int i = g.lo[q][0] + int(c / (int64_t(dy) * dz));
+  const int j = g.lo[q][1] + int((c / dz) % dy);
+  const int k = g.lo[q][2] + int(c % dz);
+  const int64_t cell = (int64_t(i) * lm.n[1] + j) * lm.n[2] + k;
+  const float org[3] = {float(i), float(j), float(k)};
+  int pi = 0;
+  int64_t o = cnt ? 0 : base + off[w];
+  const uint32_t key = cell_key(lm, i, j, k);
+  for (int att = 0; att < 32 && pi < g.nppc; ++att) {
+    float pp[3];
+    bool in = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      pp[d] = __fadd_rn(org[d], __fmul_rn(uniform01(g.seed, g.pass[q], cell, att, d), 1.0f));
+      in &= (pp[d] >= g.blo[q][d]) & (pp[d] <= g.bhi[q][d]);
+    }
+    if (!in) continue;
+    if (!cnt) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        part[d * cap + o] = pp[d];
+        part[(3 + d) * cap + o] = g.vel[q][d];
+        part[(6 + d) * cap + o] = g.vel[q][d];
+      }
+      kout[o] = key;
+      ++o;
+    }
+    ++pi;
+  }
+  if (cnt) cnt[w] = uint32_t(pi);
+}
+
+// DeleteFluidInSources on sorted particles (per-stage entry): dead keys
+__global__ void k_delete_in_regions(const float* __restrict__ part, int64_t cap,
+                                    uint32_t* __restrict__ keys, int64_t n,
+                                    const SourceRegions reg,
+                                    unsigned long long* __restrict__ ndead) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n || keys[i] == kDeadKey) return;
+  const float p[3] = {part[i], part[cap + i], part[2 * cap + i]};
+  if (in_regions(reg, p)) {
+    keys[i] = kDeadKey;
+    atomicAdd(ndead, 1ull);
+  }
+}
+
+__global__ void k_hi_keys(const unsigned long long* __restrict__ k64, uint32_t* __restrict__ k,
+                          int64_t n) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) k[i] = uint32_t(k64[i] >> 32);
+}
+
 inline unsigned nblk(int64_t n, int b) { return unsigned((n + b - 1) / b); }
+
+SourceRegions regions_at(const fsim_sim* s, float t) {
+  SourceRegions r;
+  memset(&r, 0, sizeof(r));
+  r.n = int(s->sources.size());
+  for (int q = 0; q < r.n; ++q) source_box(s->sources[size_t(q)], t, r.lo[q], r.hi[q]);
+  return r;
+}
 
 }  // namespace
 
 int launch_keys_from_positions(fsim_sim* s, int mode, float dt) {
   const int64_t n = s->n_total;
   FSIM_CK(s, cudaMemsetAsync(s->d_cnt + 3, 0, sizeof(int64_t), s->stream));
+  SourceRegions reg;
+  memset(&reg, 0, sizeof(reg));
+  if (mode == 1 && s->delete_in_sources) reg = regions_at(s, s->src_time);
+  unsigned long long* k64 = nullptr;
+  if (mode == 1 && s->composite_sort) {
+    if (n > s->cap64) {
+      for (int b = 0; b < 2; ++b) {
+        if (s->keys64[b]) cudaFree(s->keys64[b]);
+        s->keys64[b] = nullptr;
+        FSIM_CK(s, cudaMalloc(&s->keys64[b], size_t(std::max<int64_t>(n, 1)) * 8));
+      }
+      s->cap64 = n;
+    }
+    k64 = reinterpret_cast<unsigned long long*>(s->keys64[1]);
+  }
   FSIM_LAUNCH(s, "advect_keys", k_keys, nblk(n, 256), 256, 0, s->part[s->cur], s->cap_p,
               s->keys[0], s->keys[1], s->vals[1], n, s->lm, s->solid, mode, dt,
-              reinterpret_cast<unsigned long long*>(s->d_cnt + 3));
+              reinterpret_cast<unsigned long long*>(s->d_cnt + 3), reg, k64);
+  s->delete_in_sources = false;
   return FSIM_OK;
 }
 
@@ -324,6 +477,28 @@ int launch_keys_from_positions(fsim_sim* s, int mode, float dt) {
 int rebuild_topology(fsim_sim* s) {
   const int64_t n = s->n_total;
   const int bits = key_bits(s->lm);
+  if (s->composite_sort) {
+    // stable sort on (new key << 32 | old key), then the new keys back
+    unsigned long long* k64[2] = {reinterpret_cast<unsigned long long*>(s->keys64[0]),
+                                  reinterpret_cast<unsigned long long*>(s->keys64[1])};
+    size_t need = 0;
+    FSIM_CK(s, cub::DeviceRadixSort::SortPairs(nullptr, need, k64[1], k64[0], s->vals[1],
+                                               s->vals[0], n, 0, 32 + bits, s->stream));
+    if (need > s->sort_tmp_bytes) {
+      if (s->sort_tmp) cudaFree(s->sort_tmp);
+      s->sort_tmp = nullptr;
+      FSIM_CK(s, cudaMalloc(&s->sort_tmp, need));
+      s->sort_tmp_bytes = need;
+    }
+    if (n > 0) {
+      fsim::ProfScope ps(s, "radix_sort64(cub)");
+      FSIM_CK(s, cub::DeviceRadixSort::SortPairs(s->sort_tmp, need, k64[1], k64[0], s->vals[1],
+                                                 s->vals[0], n, 0, 32 + bits, s->stream));
+    }
+    FSIM_LAUNCH(s, "new_keys", k_hi_keys, nblk(n, 256), 256, 0, k64[0], s->keys[0], n);
+    s->composite_sort = false;
+    return rebuild_after_sort(s);
+  }
   // radix sort (stable)
   size_t need = 0;
   FSIM_CK(s, cub::DeviceRadixSort::SortPairs(nullptr, need, s->keys[1], s->keys[0], s->vals[1],
@@ -339,6 +514,12 @@ int rebuild_topology(fsim_sim* s) {
     FSIM_CK(s, cub::DeviceRadixSort::SortPairs(s->sort_tmp, need, s->keys[1], s->keys[0],
                                                s->vals[1], s->vals[0], n, 0, bits, s->stream));
   }
+  return rebuild_after_sort(s);
+}
+
+// keys[0]/vals[0] hold the sorted keys and permutation of n_total particles
+int rebuild_after_sort(fsim_sim* s) {
+  const int64_t n = s->n_total;
   FSIM_CK(s, cudaMemsetAsync(s->d_cnt, 0, 3 * sizeof(int64_t), s->stream));
   FSIM_LAUNCH(s, "count_live", k_count_live, nblk(n, 256), 256, 0, s->keys[0], n, s->d_cnt);
   FSIM_LAUNCH(s, "gather_particles", k_gather, nblk(n, 256), 256, 0, s->part[s->cur],
@@ -418,6 +599,91 @@ int seed_fluid(fsim_sim* s, const fsim_seed_pass* passes, int npasses, uint64_t 
               s->part[s->cur], s->cap_p, s->keys[1], s->vals[1]);
   s->n_total = total;
   return rebuild_topology(s);
+}
+
+int add_source_particles(fsim_sim* s, float t) {
+  SourceGen g;
+  memset(&g, 0, sizeof(g));
+  g.seed = s->seed;
+  g.nppc = s->cfg.nparticles_per_cell;
+  const int64_t call = s->source_calls++;
+  int64_t items = 0;
+  for (size_t q = 0; q < s->sources.size(); ++q) {
+    const fsim_source& src = s->sources[q];
+    g.begin[g.nsrc] = items;
+    if (!source_active(src, t)) continue;
+    float lo[3], hi[3];
+    source_box(src, t, lo, hi);
+    int a[3], b[3];
+    bool empty = false;
+    for (int d = 0; d < 3; ++d) {
+      // Coord(float) truncates; the domain box is [0, N-1]
+      a[d] = std::max(int(lo[d]), 0);
+      b[d] = std::min(int(hi[d]), s->lm.n[d] - 1);
+      empty |= b[d] < a[d];
+    }
+    if (empty) continue;
+    const int r = g.nsrc;
+    for (int d = 0; d < 3; ++d) {
+      g.lo[r][d] = a[d];
+      g.dim[r][d] = b[d] - a[d] + 1;
+      g.blo[r][d] = lo[d];
+      g.bhi[r][d] = hi[d];
+    }
+    source_velocity(src, t, g.vel[r]);
+    g.pass[r] = (1 << 22) + int((call & 0x1FFFF) * 32) + int(q);
+    g.begin[r] = items;
+    items += int64_t(g.dim[r][0]) * g.dim[r][1] * g.dim[r][2];
+    ++g.nsrc;
+  }
+  g.begin[g.nsrc] = items;
+  if (items == 0) return FSIM_OK;
+  // counts, exclusive scan, then the particles after the current ones
+  size_t sneed = 0;
+  uint32_t* cnt = nullptr;
+  FSIM_CK(s, cub::DeviceScan::ExclusiveSum(nullptr, sneed, cnt, cnt, int(items + 1), s->stream));
+  const size_t cnt_bytes = ((size_t(items + 1) * 4 + 255) / 256) * 256;
+  if (cnt_bytes * 2 + sneed > s->src_tmp_bytes) {
+    if (s->src_tmp) cudaFree(s->src_tmp);
+    s->src_tmp = nullptr;
+    FSIM_CK(s, cudaMalloc(&s->src_tmp, cnt_bytes * 2 + sneed));
+    s->src_tmp_bytes = cnt_bytes * 2 + sneed;
+  }
+  cnt = static_cast<uint32_t*>(s->src_tmp);
+  uint32_t* off = reinterpret_cast<uint32_t*>(static_cast<char*>(s->src_tmp) + cnt_bytes);
+  void* stmp = static_cast<char*>(s->src_tmp) + 2 * cnt_bytes;
+  FSIM_CK(s, cudaMemsetAsync(cnt, 0, size_t(items + 1) * 4, s->stream));
+  FSIM_LAUNCH(s, "source_count", k_source, nblk(items, 256), 256, 0, g, s->lm, cnt,
+              static_cast<const uint32_t*>(nullptr), s->part[s->cur], s->cap_p, int64_t(0),
+              s->keys[0]);
+  FSIM_CK(s, cub::DeviceScan::ExclusiveSum(stmp, sneed, cnt, off, int(items + 1), s->stream));
+  uint32_t added = 0;
+  FSIM_CK(s, cudaMemcpyAsync(&added, off + items, 4, cudaMemcpyDeviceToHost, s->stream));
+  FSIM_CK(s, cudaStreamSynchronize(s->stream));
+  if (added == 0) return FSIM_OK;
+  if (s->n_total + int64_t(added) > s->cap_p) {
+    // grow by a quarter more than needed (sources keep adding); the current
+    // particles and keys move over
+    const int rc = grow_particle_capacity(s, (s->n_total + int64_t(added)) * 5 / 4 + 1024);
+    if (rc) return rc;
+  }
+  FSIM_LAUNCH(s, "source_write", k_source, nblk(items, 256), 256, 0, g, s->lm,
+              static_cast<uint32_t*>(nullptr), off, s->part[s->cur], s->cap_p, s->n_total,
+              s->keys[0]);
+  s->n_total += added;
+  s->n_live = s->n_total;
+  s->composite_sort = true;
+  return FSIM_OK;
+}
+
+int delete_in_sources(fsim_sim* s, float t) {
+  if (s->sources.empty()) return FSIM_OK;
+  // dead keys are counted with DeleteOutsideParticles' (d_cnt[6]) until the next sort
+  if (!s->deleted_outside) FSIM_CK(s, cudaMemsetAsync(s->d_cnt + 6, 0, 8, s->stream));
+  FSIM_LAUNCH(s, "delete_in_sources", k_delete_in_regions, nblk(s->n_total, 256), 256, 0,
+              s->part[s->cur], s->cap_p, s->keys[0], s->n_total, regions_at(s, t),
+              reinterpret_cast<unsigned long long*>(s->d_cnt + 6));
+  return FSIM_OK;
 }
 
 int perturb(fsim_sim* s, float sigma, uint64_t seed) {

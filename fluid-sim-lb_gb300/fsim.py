@@ -63,6 +63,27 @@ class fsim_step_stats(C.Structure):
                 ("next_inv_speed", C.c_float)]
 
 
+MAX_SOURCES = 16
+SCENE_MAX_SOLIDS = 32
+
+
+class fsim_source(C.Structure):
+    _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("lo2", C.c_float * 3),
+                ("hi2", C.c_float * 3), ("box_period", C.c_float), ("velocity", C.c_float * 3),
+                ("velocity2", C.c_float * 3), ("velocity_period", C.c_float),
+                ("box_oscillating", C.c_int32), ("velocity_oscillating", C.c_int32),
+                ("timed", C.c_int32), ("start_time", C.c_float), ("end_time", C.c_float)]
+
+
+class fsim_scene(C.Structure):
+    _fields_ = [("fluid", C.c_int32), ("boundary", C.c_int32), ("gravity", C.c_float),
+                ("force", C.c_float * 3), ("nsolids", C.c_int32),
+                ("solid_lo", (C.c_int32 * 3) * SCENE_MAX_SOLIDS),
+                ("solid_hi", (C.c_int32 * 3) * SCENE_MAX_SOLIDS),
+                ("npasses", C.c_int32), ("passes", fsim_seed_pass * 8),
+                ("nsources", C.c_int32), ("sources", fsim_source * MAX_SOURCES)]
+
+
 # every symbol include/fsim.h declares, with its ctypes signature
 _P = C.c_void_p
 _SIGS = {
@@ -107,6 +128,12 @@ _SIGS = {
     "fsim_reset_kernel_times": (C.c_int, [_P]),
     "fsim_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "fsim_cfl_noalloc": (C.c_int, [_P, _P, C.POINTER(C.c_int32), C.c_float, _P, _P]),
+    "fsim_add_source": (C.c_int, [_P, C.POINTER(fsim_source)]),
+    "fsim_set_time": (C.c_int, [_P, C.c_double]),
+    "fsim_get_time": (C.c_int, [_P, C.POINTER(C.c_double)]),
+    "fsim_add_contribution_from_sources": (C.c_int, [_P, C.c_float]),
+    "fsim_delete_fluid_in_sources": (C.c_int, [_P, C.c_float]),
+    "fsim_scene_parse": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(fsim_scene)]),
     "fsim_rollout_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "fsim_rollout_destroy": (C.c_int, [_P]),
     "fsim_rollout_particle_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -183,6 +210,17 @@ def pcg_params(mode=PCG_ABSOLUTE, precision=PREC_FP32, max_iterations=1500, thre
     p.max_refinements = max_refinements
     p.threshold, p.tolerance, p.inner_tolerance = threshold, tolerance, inner_tolerance
     return p
+
+
+def parse_scene(text: str, dims) -> fsim_scene:
+    """fsim_scene_parse: an init file's text for a grid of dims cells."""
+    lib = load_library()
+    sc = fsim_scene()
+    rc = lib.fsim_scene_parse(text.encode(), (C.c_int32 * 3)(*[int(d) for d in dims]),
+                              C.byref(sc))
+    if rc:
+        raise FsimError(rc, lib.fsim_last_error(None).decode())
+    return sc
 
 
 def compute_dt(inv_speed: float, cfl: int, frame_step: float, time_in_frame: float):
@@ -264,6 +302,45 @@ class Simulation:
         for i, p in enumerate(passes):
             arr[i] = p.to_c()
         self._ck(self.lib.fsim_seed_fluid(self.h, arr, len(passes), C.c_uint64(seed)), "seed")
+
+    def seed_scene(self, scene: "fsim_scene", seed: int = 0):
+        """Seeds the passes of a parsed scene (one fsim_seed_fluid call)."""
+        self._ck(self.lib.fsim_seed_fluid(self.h, scene.passes, scene.npasses, C.c_uint64(seed)),
+                 "seed_fluid")
+
+    def add_source(self, src: fsim_source):
+        self._ck(self.lib.fsim_add_source(self.h, C.byref(src)), "add_source")
+
+    @property
+    def time(self) -> float:
+        t = C.c_double()
+        self._ck(self.lib.fsim_get_time(self.h, C.byref(t)), "get_time")
+        return t.value
+
+    @time.setter
+    def time(self, t: float):
+        self._ck(self.lib.fsim_set_time(self.h, C.c_double(t)), "set_time")
+
+    def add_contribution_from_sources(self, t: float):
+        self._ck(self.lib.fsim_add_contribution_from_sources(self.h, C.c_float(t)),
+                 "add_contribution_from_sources")
+
+    def delete_fluid_in_sources(self, t: float):
+        self._ck(self.lib.fsim_delete_fluid_in_sources(self.h, C.c_float(t)),
+                 "delete_fluid_in_sources")
+
+    @classmethod
+    def from_scene(cls, text: str, dims, flip=0.95, nppc=8, seed=0, max_particles=0, device=0):
+        """A Simulation set up as FlipDriver::Initialize sets up an init-file
+        scene: config, sources, boundary, solids, then the seeding passes."""
+        sc = parse_scene(text, dims)
+        sim = cls(dims, sc.boundary, sc.gravity, tuple(sc.force), flip, nppc, max_particles, device)
+        for q in range(sc.nsources):
+            sim.add_source(sc.sources[q])
+        for q in range(sc.nsolids):
+            sim.add_solid_cuboid(tuple(sc.solid_lo[q]), tuple(sc.solid_hi[q]))
+        sim.seed_scene(sc, seed)
+        return sim, sc
 
     def perturb_velocities(self, sigma: float, seed: int):
         self._ck(self.lib.fsim_perturb_velocities(self.h, C.c_float(sigma), C.c_uint64(seed)),

@@ -510,6 +510,13 @@ class FlipSimulation {
   void ApplyBoundaryConditions() { stage(fsim_apply_boundary_conditions(h_)); }
   void SaveGridVelocities() { stage(fsim_save_grid_velocities(h_)); }
   void DeleteOutsideParticles() { stage(fsim_delete_outside_particles(h_)); }
+  // water sources (common/flip_simulation.cc:327-329, 1207-1281); the source
+  // is already scaled to index space (FlipDriver::Initialize)
+  void AddWaterSource(const fsim_source& source) { stage(fsim_add_source(h_, &source)); }
+  void AddContributionFromSources(T t) {
+    stage(fsim_add_contribution_from_sources(h_, float(t)));
+  }
+  void DeleteFluidInSources(T t) { stage(fsim_delete_fluid_in_sources(h_, float(t))); }
   void ReinitializePhiSimple() { stage(fsim_reinitialize_phi(h_)); }
   void AddGravity(T dt) { stage(fsim_add_gravity(h_, float(dt))); }
   void ComputeDivergence() { stage(fsim_compute_divergence(h_)); }

@@ -114,6 +114,82 @@ int fsim_seed_fluid(fsim_t* sim, const fsim_seed_pass* passes, int32_t npasses,
  * (same draw for both), counter-based stream keyed by (seed, particle rank). */
 int fsim_perturb_velocities(fsim_t* sim, float sigma, uint64_t seed);
 
+/* ---- water sources ----------------------------------------------------- */
+/* application::Source<T> (common/sources.cc), already scaled to index space
+ * (boxes times the global dimensions, velocities times the scaled gravity,
+ * as FlipDriver::Initialize does, common/flip_app_sim.cc:96-104).  Restated
+ * as the reference computes it:
+ *   get_box(t) is box1 with its end lowered by 1 on every axis; the
+ *     oscillating branch of the reference writes a shadowed local and has no
+ *     effect, so an oscillating box stays box1;
+ *   get_velocity(t) is velocity1, or, when velocity_oscillating,
+ *     v1 + 0.5 (v2 - v1)(cos(pi t / box_period) + 1) (the reference uses the
+ *     box period here);
+ *   is_active(t) is start_time <= t <= end_time for timed sources, else true.
+ * At most FSIM_MAX_SOURCES sources. */
+#define FSIM_MAX_SOURCES 16
+typedef struct fsim_source {
+  float lo[3], hi[3];        /* box1 start, end */
+  float lo2[3], hi2[3];      /* box2 start, end (oscillating box) */
+  float box_period;
+  float velocity[3];         /* velocity1 */
+  float velocity2[3];
+  float velocity_period;     /* stored; see get_velocity above */
+  int32_t box_oscillating;
+  int32_t velocity_oscillating;
+  int32_t timed;
+  float start_time, end_time;
+} fsim_source;
+/* FlipSimulation::AddWaterSource, common/flip_simulation.cc:327-329 */
+int fsim_add_source(fsim_t* sim, const fsim_source* source);
+/* The simulation time sources see (the driver's advanced_time_); fsim_step
+ * reads it and then adds dt (FlipDriver::AdvanceTime). */
+int fsim_set_time(fsim_t* sim, double t);
+int fsim_get_time(fsim_t* sim, double* t);
+/* FlipSimulation::AddContributionFromSources(t), :1207-1270: every active
+ * source adds up to nparticles_per_cell particles to each cell of its box
+ * (at most 32 draws; a draw is kept inside the box), with velocity and grid
+ * velocity set to the source velocity.  Draws use the seeding generator
+ * keyed by the seed of the last fsim_seed_fluid and a per-call stream.  The
+ * grid writes of the reference are cleared by ClearGridData before any
+ * stage reads them and are not made. */
+int fsim_add_contribution_from_sources(fsim_t* sim, float t);
+/* FlipSimulation::DeleteFluidInSources(t), :1273-1281: particles inside the
+ * box of any source (active or not) are deleted. */
+int fsim_delete_fluid_in_sources(fsim_t* sim, float t);
+
+/* ---- init-file scenes --------------------------------------------------- */
+/* FlipApp::ParseSimulationConfiguration (common/flip_app.cc:159-251) and the
+ * scaling of FlipDriver::Initialize (common/flip_app_sim.cc:70-183) for a
+ * grid of dims cells.  Keys (one per line, tokens split on ", :"): fluid,
+ * boundary, gravity, force, fluid-cube, fluid-sphere, source-static,
+ * source-timed, source-oscillating, solid; other lines are ignored.
+ * Defaults: fluid 1, boundary 0, gravity 9.8, force (0,1,0).  The result is
+ * what Initialize applies, in its order: the config (scaled gravity =
+ * gravity * N1/128, force * scaled gravity), the sources (boxes * dims,
+ * velocities * scaled gravity), the boundary, the solids (cubes * dims as
+ * get_coord_bbox gives them), and the seeding passes (the fluid preset, then
+ * each additional fluid: cubes * dims with their end lowered by 1, spheres
+ * * dims, velocities * scaled gravity). */
+#define FSIM_SCENE_MAX_SOLIDS 32
+typedef struct fsim_scene {
+  int32_t fluid;            /* preset: 0 none, 1 sphere drop, 2 dam break */
+  int32_t boundary;         /* FSIM_BOUNDARY_* */
+  float gravity;            /* scaled: config gravity * N1 / 128 */
+  float force[3];           /* config force * scaled gravity */
+  int32_t nsolids;
+  int32_t solid_lo[FSIM_SCENE_MAX_SOLIDS][3];
+  int32_t solid_hi[FSIM_SCENE_MAX_SOLIDS][3];
+  int32_t npasses;
+  fsim_seed_pass passes[8];
+  int32_t nsources;
+  fsim_source sources[FSIM_MAX_SOURCES];
+} fsim_scene;
+/* text: the init file's contents.  FSIM_ERR_INVALID for a malformed line
+ * (message in fsim_last_error(NULL)) or a solid cube not on whole cells;
+ * FSIM_ERR_CAPACITY past 32 solids, 16 sources or 8 seeding passes. */
+int fsim_scene_parse(const char* text, const int32_t dims[3], fsim_scene* out);
+
 /* ---- particle I/O ------------------------------------------------------ */
 /* pos/vel/gvel are n xyz triples (AoS float[3*n]).  Upload rebins (stable
  * sort by cell in OpenVDB leaf order) and rebuilds the brick topology. */
@@ -206,7 +282,9 @@ typedef struct fsim_step_stats {
   fsim_pcg_stats pcg;
   float next_inv_speed;    /* CFL() of the velocity left by this step */
 } fsim_step_stats;
-/* MoveParticles(dt) + DeleteParticlesInSolids, ClearGridData,
+/* With sources: AddContributionFromSources(time) first and
+ * DeleteFluidInSources(time) after the move; time then advances by dt.
+ * MoveParticles(dt) + DeleteParticlesInSolids, ClearGridData,
  * TransferParticlesToGrid, ApplyBoundaryConditions, SaveGridVelocities,
  * DeleteOutsideParticles, ReinitializePhiSimple, AddGravity(dt),
  * ApplyBoundaryConditions, ComputeDivergence, PCG solve,

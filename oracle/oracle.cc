@@ -97,6 +97,12 @@ struct orc_sim {
   std::vector<float> pos, vel_p, gvel;
   std::vector<uint32_t> keys;
   std::vector<int32_t> cell;  // 3 per particle
+
+  // water sources and the driver's advanced time
+  std::vector<orc_source> sources;
+  double time = 0.0;
+  uint64_t seed = 0;          // of the last seeding (source draws use it)
+  int64_t source_calls = 0;   // draw stream of AddContributionFromSources
 };
 
 namespace {
@@ -474,6 +480,7 @@ float orc_seed_uniform(uint64_t seed, int32_t pass, int64_t cell, int32_t draw, 
 int64_t orc_seed(orc_sim* s, const orc_seed_pass* passes, int32_t npasses, uint64_t seed) {
   // FlipSimulation::InitializePhiAndParticles, flip_simulation.cc:139-188,
   // one call per pass; per-cell counts persist across passes.
+  s->seed = seed;
   const int* n = s->D.n;
   const size_t ncell = size_t(n[0]) * n[1] * n[2];
   std::vector<int32_t> count(ncell, 0);
@@ -890,10 +897,108 @@ void orc_update_particles_from_grid(orc_sim* s) {
   }
 }
 
+namespace {
+
+// Source<T>::get_box / get_velocity / is_active, common/sources.cc:66-109
+void src_box(const orc_source& q, float t, float lo[3], float hi[3]) {
+  (void)t;  // the oscillating branch assigns a shadowed local: box1 is used
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = q.lo[d];
+    hi[d] = q.hi[d] - 1.0f;  // box.set_end(box.get_end() - Vec3(1))
+  }
+}
+void src_velocity(const orc_source& q, float t, float v[3]) {
+  if (!q.velocity_oscillating) {
+    for (int d = 0; d < 3; ++d) v[d] = q.velocity[d];
+    return;
+  }
+  const float w = float(M_PI * double(t) / double(q.box_period));  // uses box_period_
+  for (int d = 0; d < 3; ++d)
+    v[d] = float(double(q.velocity[d]) +
+                 0.5 * double(q.velocity2[d] - q.velocity[d]) * (double(std::cos(w)) + 1.0));
+}
+bool src_active(const orc_source& q, float t) {
+  return !q.timed || (t >= q.start_time && t <= q.end_time);
+}
+bool in_box(const float lo[3], const float hi[3], const float p[3]) {
+  bool in = true;
+  for (int d = 0; d < 3; ++d) in &= (p[d] >= lo[d]) && (p[d] <= hi[d]);  // Cube::IsInside
+  return in;
+}
+
+}  // namespace
+
+void orc_add_source(orc_sim* s, const orc_source* src) { s->sources.push_back(*src); }
+void orc_set_time(orc_sim* s, double t) { s->time = t; }
+double orc_get_time(const orc_sim* s) { return s->time; }
+
+void orc_add_contribution_from_sources(orc_sim* s, float t) {
+  // FlipSimulation::AddContributionFromSources, flip_simulation.cc:1207-1270.
+  // Particles go to the end of their cell's list (AddParticleToData); the
+  // grid writes are cleared by ClearGridData before anything reads them.
+  const int* n = s->D.n;
+  const int64_t call = s->source_calls++;
+  bool added = false;
+  for (size_t q = 0; q < s->sources.size(); ++q) {
+    const orc_source& src = s->sources[q];
+    if (!src_active(src, t)) continue;
+    float v[3], lo[3], hi[3];
+    src_velocity(src, t, v);
+    src_box(src, t, lo, hi);
+    int a[3], b[3];
+    for (int d = 0; d < 3; ++d) {
+      a[d] = std::max(int(lo[d]), 0);            // Coord(float) truncates;
+      b[d] = std::min(int(hi[d]), n[d] - 1);     // the domain box is [0, N-1]
+    }
+    const int pass = (1 << 22) + int((call & 0x1FFFF) * 32) + int(q);
+    for (int i = a[0]; i <= b[0]; ++i)
+      for (int j = a[1]; j <= b[1]; ++j)
+        for (int k = a[2]; k <= b[2]; ++k) {
+          const float org[3] = {float(i), float(j), float(k)};
+          const int64_t c = (int64_t(i) * n[1] + j) * n[2] + k;
+          int pi = 0;
+          for (int att = 0; att < 32 && pi < s->nppc; ++att) {
+            float pp[3];
+            for (int d = 0; d < 3; ++d) pp[d] = org[d] + uniform01(s->seed, pass, c, att, d) * 1.0f;
+            if (!in_box(lo, hi, pp)) continue;
+            for (int d = 0; d < 3; ++d) {
+              s->pos.push_back(pp[d]);
+              s->vel_p.push_back(v[d]);
+              s->gvel.push_back(v[d]);
+            }
+            s->cell.push_back(i); s->cell.push_back(j); s->cell.push_back(k);
+            s->keys.push_back(s->K.key(i, j, k));
+            added = true;
+            ++pi;
+          }
+        }
+  }
+  if (added) reorder_by_key(s);  // stable: each cell's list keeps its old particles first
+}
+
+void orc_delete_fluid_in_sources(orc_sim* s, float t) {
+  // FlipSimulation::DeleteFluidInSources, flip_simulation.cc:1273-1281, with
+  // Particles::DeleteParticlesFromRegions (particles.cc:222-271): a particle
+  // inside any source's box (active or not) is removed.
+  if (s->sources.empty()) return;
+  const size_t n = s->keys.size();
+  std::vector<uint8_t> kill(n, 0);
+  for (const orc_source& src : s->sources) {
+    float lo[3], hi[3];
+    src_box(src, t, lo, hi);
+    for (size_t i = 0; i < n; ++i)
+      if (in_box(lo, hi, &s->pos[3 * i])) kill[i] = 1;
+  }
+  erase_where(s, kill);
+}
+
 int32_t orc_step(orc_sim* s, float dt, int32_t mode, int32_t precision, int32_t max_iterations,
                  double threshold, double tol, orc_pcg_stats* stats) {
-  // FlipDriver::RunOneStep, flip_app_sim.cc:211-254 (no sources)
+  // FlipDriver::RunOneStep, flip_app_sim.cc:211-254
+  const float t = float(s->time);  // advanced_time_ (T = float)
+  orc_add_contribution_from_sources(s, t);
   orc_move_particles(s, dt);
+  orc_delete_fluid_in_sources(s, t);
   orc_clear_grid(s);
   orc_transfer_particles_to_grid(s);
   orc_apply_boundary_conditions(s);
@@ -907,6 +1012,7 @@ int32_t orc_step(orc_sim* s, float dt, int32_t mode, int32_t precision, int32_t 
   orc_update_velocity_from_pressure(s);
   orc_get_velocity_update(s);
   orc_update_particles_from_grid(s);
+  s->time = double(t + dt);  // FlipDriver::AdvanceTime
   return st;
 }
 

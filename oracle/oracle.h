@@ -104,7 +104,30 @@ int32_t orc_get_velocity_update(orc_sim* s); /* 0 ok, 1 CHECK failure */
 void orc_extrapolate_to_boundary(orc_sim* s, int32_t field);
 void orc_update_particles_from_grid(orc_sim* s);
 
-/* FlipDriver::RunOneStep for one partition; returns the PCG status. */
+/* Water sources (application::Source<T>, common/sources.cc), same layout
+ * and rules as fsim_source in include/fsim.h. */
+typedef struct orc_source {
+  float lo[3], hi[3];
+  float lo2[3], hi2[3];
+  float box_period;
+  float velocity[3];
+  float velocity2[3];
+  float velocity_period;
+  int32_t box_oscillating;
+  int32_t velocity_oscillating;
+  int32_t timed;
+  float start_time, end_time;
+} orc_source;
+void orc_add_source(orc_sim* s, const orc_source* src);
+void orc_set_time(orc_sim* s, double t);
+double orc_get_time(const orc_sim* s);
+/* FlipSimulation::AddContributionFromSources(t), :1207-1270 */
+void orc_add_contribution_from_sources(orc_sim* s, float t);
+/* FlipSimulation::DeleteFluidInSources(t), :1273-1281 */
+void orc_delete_fluid_in_sources(orc_sim* s, float t);
+
+/* FlipDriver::RunOneStep for one partition (with AddSources before the move
+ * and DeleteSources after it, then time += dt); returns the PCG status. */
 int32_t orc_step(orc_sim* s, float dt, int32_t mode, int32_t precision,
                  int32_t max_iterations, double threshold, double tol,
                  orc_pcg_stats* stats);

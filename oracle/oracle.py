@@ -30,6 +30,14 @@ class orc_pcg_stats(C.Structure):
                 ("pad", C.c_int32), ("rr", C.c_double), ("bb", C.c_double)]
 
 
+class orc_source(C.Structure):
+    _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("lo2", C.c_float * 3),
+                ("hi2", C.c_float * 3), ("box_period", C.c_float), ("velocity", C.c_float * 3),
+                ("velocity2", C.c_float * 3), ("velocity_period", C.c_float),
+                ("box_oscillating", C.c_int32), ("velocity_oscillating", C.c_int32),
+                ("timed", C.c_int32), ("start_time", C.c_float), ("end_time", C.c_float)]
+
+
 _P = C.c_void_p
 _SIGS = {
     "orc_create": (_P, [C.POINTER(C.c_int32), C.c_int32, C.c_float, C.POINTER(C.c_float),
@@ -70,6 +78,11 @@ _SIGS = {
     "orc_set_divergence": (None, [_P, _P]),
     "orc_set_marker": (None, [_P, _P]),
     "orc_seed_uniform": (C.c_float, [C.c_uint64, C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
+    "orc_add_source": (None, [_P, C.POINTER(orc_source)]),
+    "orc_set_time": (None, [_P, C.c_double]),
+    "orc_get_time": (C.c_double, [_P]),
+    "orc_add_contribution_from_sources": (None, [_P, C.c_float]),
+    "orc_delete_fluid_in_sources": (None, [_P, C.c_float]),
 }
 
 _lib = None
@@ -213,6 +226,33 @@ class OracleSim:
 
     def update_particles_from_grid(self):
         self.lib.orc_update_particles_from_grid(self.h)
+
+    def add_source(self, src):
+        """src: any structure with the fsim_source / orc_source fields."""
+        o = orc_source()
+        C.memmove(C.byref(o), C.byref(src), C.sizeof(orc_source))
+        self.lib.orc_add_source(self.h, C.byref(o))
+
+    @property
+    def time(self):
+        return self.lib.orc_get_time(self.h)
+
+    @time.setter
+    def time(self, t):
+        self.lib.orc_set_time(self.h, C.c_double(t))
+
+    def add_contribution_from_sources(self, t):
+        self.lib.orc_add_contribution_from_sources(self.h, C.c_float(t))
+
+    def delete_fluid_in_sources(self, t):
+        self.lib.orc_delete_fluid_in_sources(self.h, C.c_float(t))
+
+    def seed_scene(self, scene, seed=0):
+        """Seeds the passes of a parsed fsim_scene."""
+        n = max(1, scene.npasses)
+        arr = (orc_seed_pass * n)()
+        C.memmove(arr, scene.passes, C.sizeof(orc_seed_pass) * scene.npasses)
+        return self.lib.orc_seed(self.h, arr, scene.npasses, C.c_uint64(seed))
 
     def step(self, dt, mode=0, precision=0, max_iterations=1500, threshold=0.0, tol=1e-5):
         st = orc_pcg_stats()
