@@ -5,7 +5,8 @@
 // 30-206, 211-254) sequence the FlipSimulation / PCGDriver calls, on one GPU
 // through fsim_facade.h, then repeats the same steps with the fused
 // fsim_step and reports both.  Usage:
-//   fsim_demo <N> <steps> <output_dir> [staged|fused]
+//   fsim_demo <N> <steps> <output_dir> [staged|fused] [debug]
+// "debug" also writes SaveDebugDataToFile's dumps after the last step.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -32,6 +33,7 @@ int main(int argc, char** argv) {
   const int steps = argc > 2 ? std::atoi(argv[2]) : 4;
   const std::string out = argc > 3 ? argv[3] : "demo_out";
   const bool fused = argc > 4 && std::string(argv[4]) == "fused";
+  const bool debug = argc > 5 && std::string(argv[5]) == "debug";
   const float g = float(9.8 * n);  // gravity -9.8 with dx = 1/N, index space
   const float frame_step = 1.0f / 30.0f;
 
@@ -103,6 +105,7 @@ int main(int argc, char** argv) {
   const double ms = std::chrono::duration<double, std::milli>(
                         std::chrono::steady_clock::now() - t0).count();
   sim.SaveDataToFile();
+  if (debug) sim.SaveDebugDataToFile();
   std::printf("done %d steps in %.2f ms (%s)\n", steps, ms, fused ? "fused" : "staged");
   return 0;
 }

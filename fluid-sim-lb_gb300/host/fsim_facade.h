@@ -21,6 +21,9 @@
 //  * failures throw common::FsimFailure instead of glog CHECK aborts.
 #pragma once
 
+#include <sys/stat.h>
+
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -131,6 +134,26 @@ class FieldView {
     return i >= -1 && j >= -1 && k >= -1 && i <= dims_[0] && j <= dims_[1] && k <= dims_[2];
   }
   size_t total() const { return size_t(dims_[0] + 2) * (dims_[1] + 2) * (dims_[2] + 2); }
+  // Active voxels of the box [0, dims - 1 + grow] in OpenVDB Tree3<T,3,3>
+  // iteration order: 64^3 root children in lexicographic order, then x-major
+  // 8^3 leaves, then x-major voxels.
+  std::vector<Coord> vdb_order(const std::vector<uint8_t>& on, int grow) const {
+    std::vector<Coord> out;
+    for (int i = 0; i <= dims_[0] - 1 + grow; ++i)
+      for (int j = 0; j <= dims_[1] - 1 + grow; ++j)
+        for (int k = 0; k <= dims_[2] - 1 + grow; ++k)
+          if (on[lin(i, j, k)]) out.push_back(Coord(i, j, k));
+    auto key = [](const Coord& c) {
+      uint64_t r = 0;
+      for (int d = 0; d < 3; ++d) r = (r << 16) | uint64_t(uint32_t(c[d] >> 6) & 0xFFFFu);
+      for (int d = 0; d < 3; ++d) r = (r << 3) | uint64_t((c[d] >> 3) & 7);
+      for (int d = 0; d < 3; ++d) r = (r << 3) | uint64_t(c[d] & 7);
+      return r;
+    };
+    std::stable_sort(out.begin(), out.end(),
+                     [&](const Coord& a, const Coord& b) { return key(a) < key(b); });
+    return out;
+  }
   fsim_t* h_ = nullptr;
   int field_ = -1;
   Coord dims_;
@@ -165,16 +188,17 @@ class ScalarGrid : public FieldView {
           if (isOn(i, j, k) && get(i, j, k) == value) ++n;
     return n;
   }
-  // text dump "i j k value" of active voxels (common/scalar_grid.cc:135-160)
-  void Write(const std::string& file, bool /*text*/ = true) const {
+  // ScalarGrid::Write, common/scalar_grid.cc:135-160: the box start and end,
+  // then "i j k : value" for each active voxel of the box, in OpenVDB
+  // iteration order (the text flag only selects the fopen mode there).
+  void Write(const std::string& file, bool text = true) const {
     refresh();
-    FILE* fp = std::fopen(file.c_str(), "w");
+    FILE* fp = std::fopen(file.c_str(), text ? "wt" : "wb");
     if (!fp) throw std::runtime_error("cannot open " + file);
-    for (int i = -1; i <= dims_[0]; ++i)
-      for (int j = -1; j <= dims_[1]; ++j)
-        for (int k = -1; k <= dims_[2]; ++k)
-          if (on_[lin(i, j, k)])
-            std::fprintf(fp, "%d %d %d %g\n", i, j, k, double(data_[lin(i, j, k)]));
+    std::fprintf(fp, "0 0 0\n%d %d %d\n", dims_[0] - 1, dims_[1] - 1, dims_[2] - 1);
+    for (const Coord& c : vdb_order(on_, 0)) {
+      std::fprintf(fp, "%d %d %d : %f\n", c[0], c[1], c[2], float(data_[lin(c[0], c[1], c[2])]));
+    }
     std::fclose(fp);
   }
 
@@ -219,19 +243,19 @@ class VectorGrid : public FieldView {
   bool isOn(Coord c) const { return isOn(c[0], c[1], c[2]); }
   // Applied on the device inside UpdateParticlesFromGrid (see header note).
   void ExtrapolateToBoundary() {}
-  // text dump "i j k vx vy vz" of active voxels (common/vector_grid.cc:132-160)
-  void Write(const std::string& file, bool /*text*/ = true) const {
+  // VectorGrid::Write, common/vector_grid.cc:132-160: the box start and end,
+  // then "i j k : vx vy vz" for each active voxel of the box grown by one
+  // face (staggered), in OpenVDB iteration order.
+  void Write(const std::string& file, bool text = true) const {
     refresh();
-    FILE* fp = std::fopen(file.c_str(), "w");
+    FILE* fp = std::fopen(file.c_str(), text ? "wt" : "wb");
     if (!fp) throw std::runtime_error("cannot open " + file);
-    for (int i = -1; i <= dims_[0]; ++i)
-      for (int j = -1; j <= dims_[1]; ++j)
-        for (int k = -1; k <= dims_[2]; ++k) {
-          const size_t o = lin(i, j, k);
-          if (on_[o])
-            std::fprintf(fp, "%d %d %d %g %g %g\n", i, j, k, double(data_[3 * o]),
-                         double(data_[3 * o + 1]), double(data_[3 * o + 2]));
-        }
+    std::fprintf(fp, "0 0 0\n%d %d %d\n", dims_[0] - 1, dims_[1] - 1, dims_[2] - 1);
+    for (const Coord& c : vdb_order(on_, 1)) {
+      const size_t o = lin(c[0], c[1], c[2]);
+      std::fprintf(fp, "%d %d %d : %f %f %f\n", c[0], c[1], c[2], float(data_[3 * o]),
+                   float(data_[3 * o + 1]), float(data_[3 * o + 2]));
+    }
     std::fclose(fp);
   }
 
@@ -523,6 +547,24 @@ class FlipSimulation {
   void UpdateVelocityFromPressure() { stage(fsim_update_velocity_from_pressure(h_)); }
   void GetVelocityUpdate() { stage(fsim_get_velocity_update(h_)); }
   void UpdateParticlesFromGrid() { stage(fsim_update_particles_from_grid(h_)); }
+  // FlipSimulation::SaveDebugDataToFile, common/flip_simulation.cc:1295-1316:
+  // into <output_dir>/debug, grid_velocity_%08d, grid_phi_%08d, particles_%08d
+  // (text), then grid_velocity_%08d.txt and the pressure as grid_phi_%08d.txt
+  // (the reference writes the pressure under the phi prefix).
+  void SaveDebugDataToFile() {
+    const std::string dir = output_dir_ + "/debug";
+    mkdir(output_dir_.c_str(), 0755);
+    mkdir(dir.c_str(), 0755);
+    char step[16], step_txt[24];
+    std::snprintf(step, sizeof(step), "%08d", debug_step_);
+    std::snprintf(step_txt, sizeof(step_txt), "%08d.txt", debug_step_);
+    if (grid_velocity_) grid_velocity_->Write(dir + "/grid_velocity_" + step);
+    if (grid_phi_) grid_phi_->Write(dir + "/grid_phi_" + step);
+    if (particles_) particles_->Write(dir + "/particles_" + step);
+    if (grid_velocity_) grid_velocity_->Write(dir + "/grid_velocity_" + step_txt, true);
+    if (grid_pressure_) grid_pressure_->Write(dir + "/grid_phi_" + step_txt);
+    ++debug_step_;
+  }
   // Binary particle frame particles_%08d (SaveDataToFile, :1273-1283).
   void SaveDataToFile() {
     char name[32];
@@ -620,6 +662,7 @@ class FlipSimulation {
   int boundary_ = FSIM_BOUNDARY_BOX;
   int device_ = 0;
   int frame_ = 0;
+  int debug_step_ = 0;
   bool debug_ = false;
   std::string output_dir_;
   fsim_t* h_ = nullptr;
