@@ -1371,6 +1371,43 @@ __global__ void __launch_bounds__(kThreads) k_residual64(const __grid_constant__
   if (grid_sum<2, 1>(v, a.part, a.maxb, &a.sc->cnt_r, tot) && threadIdx.x == 0) a.sc->rr = tot[0];
 }
 
+// MIXED residual replacement: r now holds the fp32 image of the fp64 true
+// residual b - A x64 and x64 has absorbed x.  x restarts at 0, the r z-face
+// planes follow r, and r.r, r.z are recomputed; CG then continues with its
+// search direction: beta = r'.z' / (r.z of the previous iteration), r.z =
+// r'.z', and the inner stop is a further inner_tolerance drop from |r'|.
+__global__ void __launch_bounds__(kThreads) k_pcg_replace(const __grid_constant__ PcgArgs a) {
+  float* x = static_cast<float*>(a.x);
+  const float* r = static_cast<const float*>(a.r);
+  Dot<1> drr, drz;
+  for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
+    for (int v = threadIdx.x; v < 512; v += kThreads) {
+      const int64_t o = int64_t(s) * 512 + v;
+      const uint8_t f = a.flags[o];
+      x[o] = 0.f;
+      const float rv = r[o];
+      const int cz = v & 7;
+      if (cz == 0 || cz == 7) {
+        const int fi = (cz == 7 ? 64 : 0) + (v >> 6) * 8 + ((v >> 3) & 7);
+        static_cast<float*>(a.zf)[int64_t(s) * 384 + fi] = rv;
+      }
+      drr.add(rv, rv);
+      drz.add(rv, tmul(inv_sel<float>(f), rv));
+    }
+  }
+  double v[2] = {drr.value(), drz.value()};
+  double tot[2];
+  if (grid_sum<1, 2>(v, a.part, a.maxb, &a.sc->cnt_s, tot) && threadIdx.x == 0) {
+    PcgScalars* sc = a.sc;
+    sc->rr = tot[0];
+    sc->beta = tot[1] / sc->rz_old;
+    sc->rz = tot[1];
+    sc->thr = sc->tol2 * tot[0];
+    sc->status = FSIM_OK;
+    sc->done = (sc->iter >= sc->max_iter) ? 1 : 0;
+  }
+}
+
 template <typename T>
 __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres, int64_t n) {
   for (int64_t o = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; o < n;
@@ -1389,7 +1426,7 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
 constexpr int kPassIters = 4;  // PCG iterations per pass of the graph's WHILE body
 
 template <typename T, int DM>
-int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl) {
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl, int par0) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -1406,8 +1443,8 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl) {
     cudaGraph_t body = np.conditional.phGraph_out[0];
     a.cond = h;
     PcgArgs ap[2] = {a, a};
-    ap[0].par = 0;
-    ap[1].par = 1;
+    ap[0].par = par0;
+    ap[1].par = par0 ^ 1;
     cudaGraphNode_t prev = nullptr;
     for (int k = 0; k < 2 * kPassIters && e == cudaSuccess; ++k) {
       cudaGraphNodeParams kn = {};
@@ -1454,9 +1491,9 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl) {
 // at once).
 template <typename T, int DM>
 int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const char* nm_spmv,
-              const char* nm_upd) {
+              const char* nm_upd, bool setup = true, int par0 = 0) {
   a.cond = 0;
-  FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
+  if (setup) FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
   const int wpb = kHotThreads / 32;
   int occ_a = 1, occ_b = 1;
   if ((s->use_pipe && sizeof(T) == 4)) {
@@ -1496,20 +1533,21 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       s->use_coop = false;
     }
   }
+  const int it0 = setup ? 0 : s->h_sc->iter;  // iterations before this segment
   if (s->use_graphs && !s->profiling) {
     int rc = FSIM_ERR_CUDA;
     if (s->use_pdl) {
-      rc = run_graph_loop<T, DM>(s, a, wgrid, true);
+      rc = run_graph_loop<T, DM>(s, a, wgrid, true, par0);
       if (rc != FSIM_OK) s->use_pdl = false;  // programmatic edges refused: plain edges
     }
-    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, false);
+    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, false, par0);
     if (rc == FSIM_OK) {
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
       // each WHILE pass runs two iterations (four kernels); the pass that
       // sees the stop flag at setup or after a breakdown also counts
-      const int64_t pairs = std::max(s->h_sc->iter + (s->h_sc->status ? 1 : 0), 1);
+      const int64_t pairs = std::max(s->h_sc->iter - it0 + (s->h_sc->status ? 1 : 0), 1);
       s->launches += 2 * kPassIters * ((pairs + kPassIters - 1) / kPassIters);
       return FSIM_OK;
     }
@@ -1517,7 +1555,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   }
   a.cond = 0;
   int chunk = 8;
-  int64_t launched = 0;  // iterations launched; the device count equals it until the stop
+  int64_t launched = par0;  // parity of the next iteration; tracks the device count
   for (;;) {
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                s->stream));
@@ -1622,30 +1660,31 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
                   unsigned(std::min<int64_t>((nvec + 255) / 256, 4096)), 256, 0, s->x64, s->pres,
                   nvec);
   } else {
-    // MIXED: fp32 inner Jacobi-PCG with exact dots; fp64 outer refinement.
+    // MIXED: fp32 Jacobi-PCG with exact dots, and fp64 residual replacement
+    // (reliable updates): each time the recursive residual has dropped by
+    // inner_tolerance, x is folded into x64, r is replaced by the fp32 image
+    // of the fp64 true residual b - A x64, and CG continues with its search
+    // direction.  The solve stops when the fp64 true residual meets the
+    // tolerance.
     if (nvec > 0) FSIM_CK(s, cudaMemsetAsync(s->x64, 0, size_t(nvec) * sizeof(double), s->stream));
-    // initial residual r = b (x64 = 0): the first inner setup computes flags
-    // and b.b exactly (fp64-accurate), which is the outer b.b.
     PcgScalars hi = h;
     hi.mode = FSIM_PCG_RELATIVE;
     hi.tol2 = prm->inner_tolerance * prm->inner_tolerance;
     const double tol2 = prm->tolerance * prm->tolerance;
     refinements = 0;
     const int max_ref = std::max(1, prm->max_refinements);
-    for (int ref = 0; ref < max_ref; ++ref) {
-      *s->h_sc = hi;
-      FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
-                                 s->stream));
-      a.init_r = (ref == 0) ? 1 : 0;
-      rc = run_inner<float, 1>(s, a, grid, "pcg_setup_mixed", "pcg_spmv_mixed",
-                               "pcg_update_mixed");
-      if (rc) return rc;
-      if (ref == 0) {
-        bb = s->h_sc->bb;
-        n_rows = int64_t(s->h_sc->n_rows);
-      }
-      total_it += s->h_sc->iter;
+    *s->h_sc = hi;
+    FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
+                               s->stream));
+    a.init_r = 1;
+    rc = run_inner<float, 1>(s, a, grid, "pcg_setup_mixed", "pcg_spmv_mixed", "pcg_update_mixed");
+    if (rc) return rc;
+    // b.b: the first setup's r.r with r = b, accumulated exactly
+    bb = s->h_sc->bb;
+    n_rows = int64_t(s->h_sc->n_rows);
+    for (;;) {
       ++refinements;
+      total_it = s->h_sc->iter;
       if (s->h_sc->status != FSIM_OK) { status = s->h_sc->status; break; }
       FSIM_LAUNCH(s, "pcg_accumulate_x64", k_accumulate_x64,
                   unsigned(std::min<int64_t>((nvec + 255) / 256, 4096)), 256, 0, a);
@@ -1655,6 +1694,11 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
       final_rr = s->h_sc->rr;
       if (final_rr <= tol2 * bb) break;
+      if (s->h_sc->iter >= prm->max_iterations || refinements >= max_ref) break;
+      FSIM_LAUNCH(s, "pcg_replace_residual", k_pcg_replace, grid, kThreads, 0, a);
+      rc = run_inner<float, 1>(s, a, grid, "pcg_setup_mixed", "pcg_spmv_mixed", "pcg_update_mixed",
+                               false, s->h_sc->iter & 1);
+      if (rc) return rc;
     }
     if (status == FSIM_OK && !(final_rr <= tol2 * bb)) status = FSIM_ERR_NOT_CONVERGED;
     FSIM_LAUNCH(s, "pcg_to_pressure", k_to_pressure<double>,
