@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "-prec-div=true", "-prec-sqrt=true",
               "-fmad=false"]
-SOURCES = ["fsim_api.cu", "k_topology.cu", "k_grid.cu", "k_pcg.cu", "k_g2p.cu", "k_noalloc.cu", "k_adjoint.cu", "scene.cu"]
+SOURCES = ["fsim_api.cu", "k_topology.cu", "k_grid.cu", "k_pcg.cu", "k_g2p.cu", "k_noalloc.cu", "k_adjoint.cu", "scene.cu", "k_levelset.cu"]
 
 
 def _nvcc() -> str:

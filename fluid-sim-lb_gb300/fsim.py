@@ -134,6 +134,7 @@ _SIGS = {
     "fsim_add_contribution_from_sources": (C.c_int, [_P, C.c_float]),
     "fsim_delete_fluid_in_sources": (C.c_int, [_P, C.c_float]),
     "fsim_scene_parse": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(fsim_scene)]),
+    "fsim_particles_to_level_set": (C.c_int, [_P, C.c_float, C.c_float, C.c_int32, _P, _P]),
     "fsim_rollout_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "fsim_rollout_destroy": (C.c_int, [_P]),
     "fsim_rollout_particle_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -437,6 +438,17 @@ class Simulation:
         act = np.empty(shp, np.uint8)
         self._ck(self.lib.fsim_download_field(self.h, which, _ptr(out), _ptr(act)), "field")
         return out, act
+
+    def level_set(self, radius=3.0, half_width=3.0, mean_iterations=1):
+        """Particles to a narrow-band level set (fsim_particles_to_level_set):
+        dense phi over voxels [-1, N] and its band mask."""
+        shp = self._dense_shape()
+        phi = np.empty(shp, np.float32)
+        act = np.empty(shp, np.uint8)
+        self._ck(self.lib.fsim_particles_to_level_set(self.h, C.c_float(radius),
+                                                      C.c_float(half_width), mean_iterations,
+                                                      _ptr(phi), _ptr(act)), "level_set")
+        return phi, act
 
     def marker(self):
         shp = self._dense_shape()

@@ -342,6 +342,22 @@ int fsim_download_leaves(fsim_t* sim, int32_t* origins, int64_t capacity,
 int fsim_cfl_noalloc(const float* vel, const uint8_t* active, const int32_t dims[3],
                      float gravity, float* inv_speed, void* stream);
 
+/* ---- particles to a level set ------------------------------------------ */
+/* The method of the reference's converter (projects/particles-to-levelset/
+ * convert.cc:80-156, OpenVDB ParticlesToLevelSet::rasterizeSpheres then
+ * LevelSetFilter::mean): each live particle is a sphere of `radius` voxels
+ * (the converter uses 3); phi at voxel point (i,j,k) is min over particles
+ * of |(i,j,k) - p| - radius, clamped to [-half_width, half_width] (OpenVDB's
+ * default band is 3); then mean_iterations passes replace every band voxel
+ * by the mean of its 3^3 neighbourhood (outside the box counts as
+ * half_width) and re-clamp.  OpenVDB's re-normalisation of the band after a
+ * filter pass is not restated.  phi (and active, |phi| < half_width) are
+ * dense host arrays in the layout of fsim_download_field; the .vdb files the
+ * converter writes are left to the caller.  No counterpart in the library
+ * path of the reference (it is a separate tool). */
+int fsim_particles_to_level_set(fsim_t* sim, float radius, float half_width,
+                                int32_t mean_iterations, float* phi, uint8_t* active);
+
 /* ---- differentiable rollout (adjoint of projection and advection) ------ */
 /* No counterpart in the reference (the reference has no gradients).  A
  * rollout of `steps` FLIP steps (the fsim_step sequence, box boundary) at a
