@@ -689,6 +689,37 @@ int fsim_step(fsim_t* s, float dt, const fsim_pcg_params* prm, fsim_step_stats* 
   return FSIM_OK;
 }
 
+int fsim_run_frames(fsim_t* s, int32_t nframes, float frame_rate, int32_t cfl,
+                    const fsim_pcg_params* prm, fsim_frame_fn on_frame, void* user,
+                    fsim_run_stats* st) {
+  if (!s || !prm || nframes < 0 || !(frame_rate > 0.f) || cfl < 1) return FSIM_ERR_INVALID;
+  cudaSetDevice(s->dev);
+  fsim_run_stats acc;
+  std::memset(&acc, 0, sizeof(acc));
+  const float frame_step = 1.0f / frame_rate;  // params_.frame_step = T(1)/T(frame_rate)
+  float inv = 0.f;
+  int rc = fsim_cfl(s, &inv);
+  if (rc) return rc;
+  for (int f = 0; f < nframes; ++f) {
+    float step = 0.f;  // ResetDt
+    while (double(step) + 1e-5 < double(frame_step)) {
+      float dt = 0.f;
+      fsim_compute_dt(inv, cfl, frame_step, &step, &dt);
+      fsim_step_stats ss;
+      if ((rc = fsim_step(s, dt, prm, &ss))) return rc;
+      inv = ss.next_inv_speed;
+      acc.steps += 1;
+      acc.pcg_iterations += ss.pcg.iterations;
+      acc.last_dt = dt;
+    }
+    acc.frames += 1;
+    if (on_frame) on_frame(s, f, user);
+  }
+  acc.time = s->time;
+  if (st) *st = acc;
+  return FSIM_OK;
+}
+
 int fsim_compute_dt(float inv_speed, int32_t cfl, float frame_step, float* time_in_frame,
                     float* dt_out) {
   if (!time_in_frame || !dt_out || !(frame_step > 0.f)) return FSIM_ERR_INVALID;

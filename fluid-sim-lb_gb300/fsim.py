@@ -67,6 +67,14 @@ MAX_SOURCES = 16
 SCENE_MAX_SOLIDS = 32
 
 
+class fsim_run_stats(C.Structure):
+    _fields_ = [("frames", C.c_int32), ("steps", C.c_int32), ("pcg_iterations", C.c_int64),
+                ("time", C.c_double), ("last_dt", C.c_float)]
+
+
+FRAME_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int32, C.c_void_p)
+
+
 class fsim_source(C.Structure):
     _fields_ = [("lo", C.c_float * 3), ("hi", C.c_float * 3), ("lo2", C.c_float * 3),
                 ("hi2", C.c_float * 3), ("box_period", C.c_float), ("velocity", C.c_float * 3),
@@ -135,6 +143,8 @@ _SIGS = {
     "fsim_delete_fluid_in_sources": (C.c_int, [_P, C.c_float]),
     "fsim_scene_parse": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(fsim_scene)]),
     "fsim_particles_to_level_set": (C.c_int, [_P, C.c_float, C.c_float, C.c_int32, _P, _P]),
+    "fsim_run_frames": (C.c_int, [_P, C.c_int32, C.c_float, C.c_int32, C.POINTER(fsim_pcg_params),
+                                  FRAME_FN, _P, C.POINTER(fsim_run_stats)]),
     "fsim_rollout_create": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "fsim_rollout_destroy": (C.c_int, [_P]),
     "fsim_rollout_particle_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -438,6 +448,15 @@ class Simulation:
         act = np.empty(shp, np.uint8)
         self._ck(self.lib.fsim_download_field(self.h, which, _ptr(out), _ptr(act)), "field")
         return out, act
+
+    def run_frames(self, nframes: int, params: fsim_pcg_params, frame_rate=30.0, cfl=1,
+                   on_frame=None) -> fsim_run_stats:
+        """The driver's frame loop (fsim_run_frames); on_frame(frame) after each frame."""
+        cb = FRAME_FN(lambda h, f, u: on_frame(int(f))) if on_frame else FRAME_FN()
+        st = fsim_run_stats()
+        self._ck(self.lib.fsim_run_frames(self.h, nframes, C.c_float(frame_rate), cfl,
+                                          C.byref(params), cb, None, C.byref(st)), "run_frames")
+        return st
 
     def level_set(self, radius=3.0, half_width=3.0, mean_iterations=1):
         """Particles to a narrow-band level set (fsim_particles_to_level_set):

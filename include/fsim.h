@@ -300,6 +300,27 @@ int fsim_step(fsim_t* sim, float dt, const fsim_pcg_params* params,
 int fsim_compute_dt(float inv_speed, int32_t cfl, float frame_step,
                     float* time_in_frame, float* dt);
 
+/* The frame loop of the reference's driver (SimulationDriver::RunSimulation,
+ * projects/flip-current-lb/water_app.cc:68-86, with WhileAndComputeDt and
+ * AdvanceTime, common/flip_app_sim.cc:357-462): for each of nframes frames
+ * of 1/frame_rate, steps run while time_in_frame + 1e-5 < frame step, each
+ * with dt from the rule of fsim_compute_dt on CFL() of the previous step's
+ * velocity (fsim_cfl before the first step).  on_frame (nullable) is called
+ * after each frame (SaveData's place).  The loop is driven from the host:
+ * each step rebuilds the leaf topology, whose counts size the next launches,
+ * so a step cannot be one graph. */
+typedef void (*fsim_frame_fn)(fsim_t* sim, int32_t frame, void* user);
+typedef struct fsim_run_stats {
+  int32_t frames;
+  int32_t steps;
+  int64_t pcg_iterations;
+  double time;            /* the handle's time after the loop */
+  float last_dt;
+} fsim_run_stats;
+int fsim_run_frames(fsim_t* sim, int32_t nframes, float frame_rate, int32_t cfl,
+                    const fsim_pcg_params* params, fsim_frame_fn on_frame, void* user,
+                    fsim_run_stats* stats);
+
 /* ---- dense downloads (parity / output) -------------------------------- */
 enum {
   FSIM_FIELD_VELOCITY = 0,        /* grid_velocity_ (Vec3) */

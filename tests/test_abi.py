@@ -83,7 +83,8 @@ def test_struct_layouts_match_header(tmp_path):
     if not shutil.which("gcc"):
         pytest.skip("gcc unavailable")
     structs = [fsim.fsim_config, fsim.fsim_shape, fsim.fsim_seed_pass, fsim.fsim_pcg_params,
-               fsim.fsim_pcg_stats, fsim.fsim_step_stats, fsim.fsim_source, fsim.fsim_scene]
+               fsim.fsim_pcg_stats, fsim.fsim_step_stats, fsim.fsim_source, fsim.fsim_scene,
+               fsim.fsim_run_stats]
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fsim.h"', "int main(void){"]
     for st in structs:
         n = st.__name__

@@ -242,3 +242,33 @@ def test_step_deterministic():
     assert np.array_equal(outs[0][4], outs[1][4])
     assert rel_l2(outs[0][1], outs[1][1]) <= FIELD_RTOL
     assert rel_l2(outs[0][3], outs[1][3]) <= FIELD_RTOL
+
+
+def test_run_frames_equals_stepping_by_hand():
+    """fsim_run_frames is the driver's frame loop: the same dt sequence and
+    state as fsim_compute_dt + fsim_step called by hand."""
+    orc = make_oracle(24, "sphere_drop")
+    a = make_gpu(orc)
+    b = make_gpu(orc)
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 1500, tolerance=1e-5)
+    frames = []
+    st = a.run_frames(2, prm, frame_rate=30.0, on_frame=frames.append)
+    assert frames == [0, 1] and st.frames == 2
+    inv = b.cfl()
+    steps, its = 0, 0
+    frame_step = float(np.float32(1.0) / np.float32(30.0))
+    for _ in range(2):
+        t = 0.0
+        while t + 1e-5 < frame_step:
+            dt, t = fsim.compute_dt(inv, 1, frame_step, t)
+            s = b.step(dt, prm)
+            inv = s.next_inv_speed
+            steps += 1
+            its += s.pcg.iterations
+    assert st.steps == steps and st.pcg_iterations == its
+    pa, va, ga = a.download_particles()
+    pb, vb, gb = b.download_particles()
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    assert a.time == pytest.approx(b.time)
+    a.close()
+    b.close()
