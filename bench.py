@@ -235,34 +235,43 @@ def run_gpu(args, rank, world):
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     barrier()
     torch.cuda.synchronize()
+    import ctypes as C
+
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    marks = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
     e0.record(stream)
-    for _ in range(e2e_steps):
-        sim.lib.fsim_upload_particles(sim.h, hp.data_ptr(), hv.data_ptr(), hg.data_ptr(),
-                                      hp.shape[0])
+    for k in range(e2e_steps):
+        marks[k][0].record(stream)
+        rc = sim.lib.fsim_upload_particles(sim.h, hp.data_ptr(), hv.data_ptr(), hg.data_ptr(),
+                                           hp.shape[0])
+        if rc:
+            raise RuntimeError(sim.lib.fsim_last_error(sim.h).decode())
+        marks[k][1].record(stream)
         st = sim.step(next_dt(), prm)
         inv = st.next_inv_speed
         cnt = sim.particle_count()
-        import ctypes as C
-
+        marks[k][2].record(stream)
         got = C.c_int64()
         rc = sim.lib.fsim_download_particles(sim.h, hp.data_ptr(), hv.data_ptr(), hg.data_ptr(),
                                              hp.shape[0], C.byref(got))
         if rc:
             raise RuntimeError(sim.lib.fsim_last_error(sim.h).decode())
+        marks[k][3].record(stream)
         if cnt < hp.shape[0]:  # particles deleted at walls: shrink the state
             hp, hv, hg = hp[:cnt], hv[:cnt], hg[:cnt]
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_split = {name: sum(m[i].elapsed_time(m[i + 1]) for m in marks) / e2e_steps
+                 for i, name in enumerate(("upload_ms", "step_ms", "download_ms"))}
     barrier()
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], device=f"cuda:{device}")
     sim.close()
     return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, clocks=clk.summary(),
                 device_memory_gb=(total_b - free_b) / 1e9,
                 piters=piters, prows=prows, prof_ms=prof_ms,
-                n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms,
+                n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms, e2e_split=e2e_split,
                 e2e_bytes=36 * n_particles)
 
 
@@ -619,7 +628,8 @@ def main():
                                                  pcg_iters_per_step=float(np.mean(res["iters"]))),
             "roofline": roofline(res),
             "e2e": {"value": whole_job_rate(world, 1, res["e2e_ms"]), "unit": "steps/s",
-                    "h2d_bytes_per_step": res["e2e_bytes"], "d2h_bytes_per_step": res["e2e_bytes"]},
+                    "h2d_bytes_per_step": res["e2e_bytes"], "d2h_bytes_per_step": res["e2e_bytes"],
+                    **{k: round(v, 3) for k, v in res["e2e_split"].items()}},
             "gpu_launches": res["launches"], "clocks": res["clocks"],
             "device_memory_gb": round(res["device_memory_gb"], 2),
             "kernels_ms": {k: round(v[0], 3) for k, v in sorted(res["kt"].items(),

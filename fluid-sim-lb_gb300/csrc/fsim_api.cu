@@ -424,15 +424,13 @@ int fsim_upload_particles(fsim_t* s, const float* pos, const float* vel, const f
   }
   s->n_total = n;
   if ((rc = launch_keys_from_positions(s, 0, 0.f))) return rc;
-  FSIM_CK(s, cudaMemcpyAsync(s->h_cnt + 3, s->d_cnt + 3, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                             s->stream));
-  FSIM_CK(s, cudaStreamSynchronize(s->stream));
-  if (s->h_cnt[3] != 0) {
+  int64_t invalid = 0;
+  if ((rc = rebin_uploaded(s, &invalid))) return rc;
+  if (invalid != 0) {
     s->n_total = 0;
     s->have_topology = false;
     return fail(s, FSIM_ERR_INVALID, "particle positions must lie in [0, N] per axis");
   }
-  if ((rc = rebuild_topology(s))) return rc;
   return after_sort(s);
 }
 
@@ -465,15 +463,24 @@ int fsim_download_particles(fsim_t* s, float* pos, float* vel, float* gvel, int6
     FSIM_CK(s, cudaMemcpyAsync(keys.data(), s->keys[0], size_t(nl) * 4, cudaMemcpyDeviceToHost,
                                s->stream));
   }
+  if (!s->deleted_outside) {
+    // all three fields: convert into their own staging slices, copy, one sync
+    for (int f = 0; f < 3; ++f) {
+      if (!outs[f]) continue;
+      float* st = stage + size_t(f) * 3 * s->cap_p;
+      FSIM_LAUNCH(s, "soa_to_aos", k_soa_to_aos, unsigned((nl + 255) / 256), 256, 0,
+                  s->part[s->cur], st, nl, s->cap_p, 3 * f);
+      FSIM_CK(s, cudaMemcpyAsync(outs[f], st, size_t(nl) * 12, cudaMemcpyDeviceToHost,
+                                 s->stream));
+    }
+    FSIM_CK(s, cudaStreamSynchronize(s->stream));
+    return FSIM_OK;
+  }
   for (int f = 0; f < 3; ++f) {
     if (!outs[f]) continue;
     FSIM_LAUNCH(s, "soa_to_aos", k_soa_to_aos, unsigned((nl + 255) / 256), 256, 0,
                 s->part[s->cur], stage, nl, s->cap_p, 3 * f);
-    if (!s->deleted_outside) {
-      FSIM_CK(s, cudaMemcpyAsync(outs[f], stage, size_t(nl) * 12, cudaMemcpyDeviceToHost,
-                                 s->stream));
-      FSIM_CK(s, cudaStreamSynchronize(s->stream));
-    } else {
+    {
       std::vector<float> tmp(size_t(nl) * 3);
       FSIM_CK(s, cudaMemcpyAsync(tmp.data(), stage, size_t(nl) * 12, cudaMemcpyDeviceToHost,
                                  s->stream));

@@ -312,7 +312,10 @@ int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf);
 // particle arrays for at least n particles (the current ones are kept)
 int grow_particle_capacity(fsim_sim* s, int64_t n);
 int rebuild_topology(fsim_sim* s);  // from keys[cur]/vals, n_total
-int rebuild_after_sort(fsim_sim* s);  // the topology part, keys[0]/vals[0] sorted
+// the topology part, keys[0]/vals[0] sorted; gather: permute the particles by vals[0]
+int rebuild_after_sort(fsim_sim* s, bool gather = true);
+// upload: rebin the particles whose keys are in keys[1] (sort skipped when sorted)
+int rebin_uploaded(fsim_sim* s, int64_t* invalid);
 
 // kernel entry points implemented in the .cu files
 int launch_keys_from_positions(fsim_sim* s, int mode, float dt);

@@ -429,6 +429,13 @@ __global__ void k_delete_in_regions(const float* __restrict__ part, int64_t cap,
   }
 }
 
+// adjacent pairs out of order (k[i] > k[i+1])
+__global__ void k_count_desc(const uint32_t* __restrict__ k, int64_t n,
+                             unsigned long long* __restrict__ cnt) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i + 1 < n && k[i] > k[i + 1]) atomicAdd(cnt, 1ull);
+}
+
 __global__ void k_hi_keys(const unsigned long long* __restrict__ k64, uint32_t* __restrict__ k,
                           int64_t n) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -518,13 +525,15 @@ int rebuild_topology(fsim_sim* s) {
 }
 
 // keys[0]/vals[0] hold the sorted keys and permutation of n_total particles
-int rebuild_after_sort(fsim_sim* s) {
+int rebuild_after_sort(fsim_sim* s, bool gather) {
   const int64_t n = s->n_total;
   FSIM_CK(s, cudaMemsetAsync(s->d_cnt, 0, 3 * sizeof(int64_t), s->stream));
   FSIM_LAUNCH(s, "count_live", k_count_live, nblk(n, 256), 256, 0, s->keys[0], n, s->d_cnt);
-  FSIM_LAUNCH(s, "gather_particles", k_gather, nblk(n, 256), 256, 0, s->part[s->cur],
-              s->part[s->cur ^ 1], s->cap_p, s->vals[0], s->d_cnt);
-  s->cur ^= 1;
+  if (gather) {
+    FSIM_LAUNCH(s, "gather_particles", k_gather, nblk(n, 256), 256, 0, s->part[s->cur],
+                s->part[s->cur ^ 1], s->cap_p, s->vals[0], s->d_cnt);
+    s->cur ^= 1;
+  }
   // leaves
   const uint32_t D = s->lm.dense;
   FSIM_CK(s, cudaMemsetAsync(s->d_flag, 0, D, s->stream));
@@ -598,6 +607,27 @@ int seed_fluid(fsim_sim* s, const fsim_seed_pass* passes, int npasses, uint64_t 
   FSIM_LAUNCH(s, "seed_write", k_seed, nblk(ncell, 256), 256, 0, a, s->lm, s->solid, 1, ctr,
               s->part[s->cur], s->cap_p, s->keys[1], s->vals[1]);
   s->n_total = total;
+  return rebuild_topology(s);
+}
+
+// Upload helper: keys (mode 0) are in keys[1]; when they are already in cell
+// order (particles that came from a download) the sort and the gather are
+// skipped.  Returns FSIM_OK and sets *invalid to the number of positions
+// outside [0, N].
+int rebin_uploaded(fsim_sim* s, int64_t* invalid) {
+  const int64_t n = s->n_total;
+  FSIM_CK(s, cudaMemsetAsync(s->d_cnt + 7, 0, sizeof(int64_t), s->stream));
+  FSIM_LAUNCH(s, "count_unsorted", k_count_desc, nblk(n, 256), 256, 0, s->keys[1], n,
+              reinterpret_cast<unsigned long long*>(s->d_cnt + 7));
+  FSIM_CK(s, cudaMemcpyAsync(s->h_cnt + 3, s->d_cnt + 3, 5 * sizeof(int64_t),
+                             cudaMemcpyDeviceToHost, s->stream));
+  FSIM_CK(s, cudaStreamSynchronize(s->stream));
+  *invalid = s->h_cnt[3];
+  if (*invalid) return FSIM_OK;
+  if (s->h_cnt[7] == 0) {
+    std::swap(s->keys[0], s->keys[1]);  // sorted already: keep the order
+    return rebuild_after_sort(s, false);
+  }
   return rebuild_topology(s);
 }
 
