@@ -144,7 +144,7 @@ def pcg_cfg(args):
 
     prec = {"fp32": fsim.PREC_FP32, "mixed": fsim.PREC_MIXED, "fp64": fsim.PREC_FP64}[args.precision]
     return fsim.pcg_params(fsim.PCG_RELATIVE, prec, args.max_iterations, tolerance=args.tol,
-                           inner_tolerance=1e-3)
+                           inner_tolerance=1e-2)
 
 
 def make_sim(wl, args, device):
@@ -405,7 +405,7 @@ def pcg_compare(args):
                                            tolerance=tol))
         out["fp32"].append({"tol": tol, "ms": ms, "iterations": stt.iterations,
                             "status": stt.status, "error": float(np.linalg.norm(x - xref) / nref)})
-    for tol, inner in ((1e-6, 1e-2), (1e-7, 1e-2), (1e-8, 1e-3), (1e-9, 1e-3)):
+    for tol, inner in ((1e-6, 1e-2), (1e-6, 1e-3), (1e-7, 1e-2), (1e-8, 1e-3), (1e-9, 1e-3)):
         ms, stt, x = solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 40000,
                                            tolerance=tol, inner_tolerance=inner,
                                            max_refinements=20))

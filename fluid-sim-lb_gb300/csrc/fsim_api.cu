@@ -597,7 +597,7 @@ int fsim_pcg_default_params(const fsim_t* s, fsim_pcg_params* p) {
   const int volume = s->lm.n[0] * s->lm.n[1] * s->lm.n[2];
   p->threshold = double(float(volume) * float(0.5 * 1e-8));
   p->tolerance = 1e-5;
-  p->inner_tolerance = 1e-3;
+  p->inner_tolerance = 1e-2;
   return FSIM_OK;
 }
 

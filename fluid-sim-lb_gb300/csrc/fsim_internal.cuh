@@ -147,6 +147,7 @@ struct PcgScalars {
   int mode, fp32;  // FSIM_PCG_* ; fp32 != 0: scalars are rounded to float
   double thr;      // ABSOLUTE: r.r threshold; RELATIVE: set to tol2*bb
   double tol2;     // RELATIVE: tolerance squared
+  double tol2_outer;  // MIXED: outer tolerance squared; a segment never stops below tol2_outer*bb
   unsigned int cnt_a, cnt_b, cnt_s, cnt_r;
   unsigned long long n_rows;  // FLUID cells (unknowns), counted by setup
   // grid barrier of the persistent (cooperative) PCG loop

@@ -1375,7 +1375,9 @@ __global__ void __launch_bounds__(kThreads) k_residual64(const __grid_constant__
 // residual b - A x64 and x64 has absorbed x.  x restarts at 0, the r z-face
 // planes follow r, and r.r, r.z are recomputed; CG then continues with its
 // search direction: beta = r'.z' / (r.z of the previous iteration), r.z =
-// r'.z', and the inner stop is a further inner_tolerance drop from |r'|.
+// r'.z', and the inner stop is a further inner_tolerance drop from |r'|, but
+// no lower than the outer target: iterating past tol*|b| in fp32 only
+// overshoots, because the fp64 check that follows decides convergence.
 __global__ void __launch_bounds__(kThreads) k_pcg_replace(const __grid_constant__ PcgArgs a) {
   float* x = static_cast<float*>(a.x);
   const float* r = static_cast<const float*>(a.r);
@@ -1402,7 +1404,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_replace(const __grid_constant_
     sc->rr = tot[0];
     sc->beta = tot[1] / sc->rz_old;
     sc->rz = tot[1];
-    sc->thr = sc->tol2 * tot[0];
+    sc->thr = fmax(sc->tol2 * tot[0], sc->tol2_outer * sc->bb);
     sc->status = FSIM_OK;
     sc->done = (sc->iter >= sc->max_iter) ? 1 : 0;
   }
@@ -1671,6 +1673,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
     hi.mode = FSIM_PCG_RELATIVE;
     hi.tol2 = prm->inner_tolerance * prm->inner_tolerance;
     const double tol2 = prm->tolerance * prm->tolerance;
+    hi.tol2_outer = tol2;
     refinements = 0;
     const int max_ref = std::max(1, prm->max_refinements);
     *s->h_sc = hi;

@@ -215,7 +215,7 @@ class SeedPass:
 
 
 def pcg_params(mode=PCG_ABSOLUTE, precision=PREC_FP32, max_iterations=1500, threshold=0.0,
-               tolerance=1e-5, inner_tolerance=1e-3, max_refinements=8) -> fsim_pcg_params:
+               tolerance=1e-5, inner_tolerance=1e-2, max_refinements=8) -> fsim_pcg_params:
     p = fsim_pcg_params()
     p.mode, p.precision, p.max_iterations = mode, precision, max_iterations
     p.max_refinements = max_refinements

@@ -250,11 +250,13 @@ enum {
 typedef struct fsim_pcg_params {
   int32_t mode;            /* FSIM_PCG_* */
   int32_t precision;       /* FSIM_PREC_* */
-  int32_t max_iterations;  /* per inner solve (reference default 1500) */
+  int32_t max_iterations;  /* all inner iterations of one solve (reference default 1500) */
   int32_t max_refinements; /* MIXED: outer refinement sweeps (>=1) */
   double threshold;        /* ABSOLUTE: r.r threshold (reference N^3*0.5e-8) */
   double tolerance;        /* RELATIVE: ||r||/||b|| target (outer, MIXED) */
-  double inner_tolerance;  /* MIXED: relative target of each inner solve */
+  double inner_tolerance;  /* MIXED: drop of the fp32 recursive residual between fp64
+                              residual replacements; no segment iterates below
+                              tolerance*||b||, where the fp64 check decides */
 } fsim_pcg_params;
 typedef struct fsim_pcg_stats {
   int32_t iterations;      /* total inner iterations */

@@ -76,6 +76,27 @@ def test_mixed_matches_fp64_oracle():
     sim.close()
 
 
+def test_mixed_segments_stop_at_the_outer_target():
+    """Inner segments drop the recursive residual by inner_tolerance between
+    fp64 replacements, but none iterates below tolerance*|b|: with inner 1e-3
+    and tolerance 1e-7 the third segment stops at 1e-7, not 1e-9, and MIXED
+    needs about FP64's iteration count."""
+    orc, sim = _prepared(n=64)
+    st64 = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP64, 20000,
+                                         tolerance=1e-7))
+    x64, _ = sim.field(fsim.FIELD_PRESSURE)
+    for inner in (1e-2, 1e-3):
+        st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 20000,
+                                           tolerance=1e-7, inner_tolerance=inner,
+                                           max_refinements=20))
+        assert st.status == 0 and np.sqrt(st.rr / st.bb) <= 1e-7
+        assert st.iterations <= 1.1 * st64.iterations + 5, (inner, st.iterations,
+                                                            st64.iterations)
+        a, _ = sim.field(fsim.FIELD_PRESSURE)
+        assert rel_l2(a, x64) <= 1e-5
+    sim.close()
+
+
 def test_fp64_matches_fp64_oracle():
     orc, sim = _prepared(n=24, scene="sphere_drop")
     ost = orc.pcg_solve(mode=1, precision=2, max_iterations=20000, tol=1e-12)
