@@ -242,14 +242,9 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   s->dev = cfg->device;
   if (cudaSetDevice(s->dev) != cudaSuccess) { delete s; return FSIM_ERR_CUDA; }
   cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->dev);
-  s->max_blocks = std::max(1, s->num_sms) * 16;
-  // FSIM_PCG_GRAPH=0 turns the graph loop off (host polling); unset or 1:
-  // graph with plain edges; 2: graph with programmatic (early-launch) edges,
-  // which measured about 3% slower per iteration at 256^3.
-  if (const char* g = std::getenv("FSIM_PCG_GRAPH")) {
-    s->use_graphs = g[0] != '0';
-    s->use_pdl = g[0] == '2';
-  }
+  s->max_blocks = std::max(1, s->num_sms) * 16;  // a multiple of 4: partial rows stay 16-byte aligned
+  // FSIM_PCG_GRAPH=0 turns the graph loop off (host polling)
+  if (const char* g = std::getenv("FSIM_PCG_GRAPH")) s->use_graphs = g[0] != '0';
   // FSIM_PCG_COOP=1: the PCG iterations as one persistent cooperative kernel
   if (const char* c = std::getenv("FSIM_PCG_COOP")) s->use_coop = c[0] == '1';
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels
@@ -278,6 +273,7 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if ((rc = dmalloc(s, &s->d_cnt, 16))) return bail(rc);
   if ((rc = dmalloc(s, &s->d_sc, 1))) return bail(rc);
   if ((rc = dmalloc(s, &s->d_part, size_t(s->max_blocks) * 4))) return bail(rc);
+  if ((rc = dmalloc(s, &s->d_partf, size_t(s->max_blocks) * 8))) return bail(rc);
   if (cudaMallocHost(&s->h_cnt, 16 * sizeof(int64_t)) != cudaSuccess) return bail(FSIM_ERR_CUDA);
   if (cudaMallocHost(&s->h_sc, sizeof(PcgScalars)) != cudaSuccess) return bail(FSIM_ERR_CUDA);
   cudaMemsetAsync(s->d_cnt, 0, 16 * sizeof(int64_t), s->stream);

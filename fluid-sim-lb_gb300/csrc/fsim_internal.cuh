@@ -140,19 +140,31 @@ __host__ __device__ inline bool extrap_activated(const int n[3], int i, int j, i
 // PCG flags byte per cell: bit0 FLUID, bits1..3 diag (# non-solid neighbours).
 __host__ __device__ inline int flag_diag(uint8_t f) { return (f >> 1) & 7; }
 
-// Device scalar block of one PCG solve.
-struct PcgScalars {
+// State handed from one hot PCG kernel to the next (see k_pcg.cu): the
+// residual dots and beta when they are given (after setup or a residual
+// replacement) instead of summed from the previous kernel's partials.
+struct PcgIterState {
+  double rr, rz, beta, rz_prev;
+  int iter, done, status, given;
+};
+
+// Device scalar block of one PCG solve (16-byte multiple: the hot kernels
+// copy it to shared memory in 16-byte pieces).
+struct alignas(16) PcgScalars {
   double rz, rz_old, rr, pAp, bb, alpha, beta, rr0;
   int iter, done, status, max_iter;
   int mode, fp32;  // FSIM_PCG_* ; fp32 != 0: scalars are rounded to float
   double thr;      // ABSOLUTE: r.r threshold; RELATIVE: set to tol2*bb
   double tol2;     // RELATIVE: tolerance squared
   double tol2_outer;  // MIXED: outer tolerance squared; a segment never stops below tol2_outer*bb
-  unsigned int cnt_a, cnt_b, cnt_s, cnt_r;
+  unsigned int cnt_s, cnt_r;
   unsigned long long n_rows;  // FLUID cells (unknowns), counted by setup
   // grid barrier of the persistent (cooperative) PCG loop
   unsigned int bar_count, bar_gen, bar_err, bar_pad;
   double bar_tot[2];  // totals the barrier's last block publishes
+  // hot-loop hand-off: [0] spmv -> update, [1] update -> spmv (and setup /
+  // residual replacement -> spmv)
+  PcgIterState st[2];
 };
 
 struct DevMem {
@@ -233,7 +245,7 @@ struct fsim_sim {
   double* b64 = nullptr;
   fsim::PcgScalars* d_sc = nullptr;
   double* d_part = nullptr;  // block partials (3 * max_blocks)
-  float* d_partf = nullptr;
+  float* d_partf = nullptr;  // fp32 / double-float partials of the hot PCG kernels (8 * max_blocks)
   int max_blocks = 0;
 
   // misc device scalars: [0] n_live [1] n_pleaf [2] n_gleaf [3] invalid
@@ -253,10 +265,8 @@ struct fsim_sim {
   bool weight_valid = false;
   bool deleted_outside = false;
 
-  // PCG iterations as a CUDA graph with a conditional WHILE node, its
-  // kernels joined by programmatic (early-launch) edges
+  // PCG iterations as a CUDA graph with a conditional WHILE node
   bool use_graphs = true;
-  bool use_pdl = false;
   // PCG iterations as one cooperative persistent kernel with grid barriers
   // (measured slower than the graph loop at 256^3: 42.5 vs 38.9 us per
   // iteration; opt-in)

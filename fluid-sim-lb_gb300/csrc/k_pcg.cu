@@ -12,11 +12,14 @@
 // +z,+y,+x), which makes it bit-identical to the oracle for identical p.
 //
 // Per iteration two kernels run back to back on device-resident scalars:
-//   spmv:   p_j = z_j + beta_{j-1} p_{j-1} (z = r/diag recomputed, never
-//           stored), p_j.(A p_j); the last CTA forms alpha.
-//   update: A p_j recomputed from p_j (Ap is never stored), x += alpha p,
-//           r -= alpha Ap, r.r and r.z; the last CTA forms beta, counts the
-//           iteration and sets the stop flag.
+//   spmv:   head: beta_{j-1} from the previous update's r.r, r.z partials
+//           and the loop test; then p_j = z_j + beta_{j-1} p_{j-1} (z =
+//           r/diag recomputed, never stored) and p_j.(A p_j) partials.
+//   update: head: alpha from the spmv's p.Ap partials; then A p_j
+//           recomputed from p_j (Ap is never stored), x += alpha p,
+//           r -= alpha Ap, and r.r, r.z partials.
+// Every CTA of a kernel sums its predecessor's partials itself (in one fixed
+// order), so no last-CTA reduction separates two launches.
 // HBM bytes per unknown per iteration: spmv reads r, p_{j-1}, flags and
 // writes p_j (13 B); update reads p_j, x, r, flags and writes x, r (21 B).
 // Each warp owns half a leaf: a lane holds one z-column of 8 cells in
@@ -30,6 +33,7 @@
 // r = b - A x with x kept in fp64) and FP64 (fp64 vectors and dots).
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "fsim_internal.cuh"
 
@@ -80,6 +84,7 @@ struct Dot<0> {
   float s = 0.f;
   __device__ void add(float a, float b) { s = __fadd_rn(s, __fmul_rn(a, b)); }
   __device__ double value() const { return double(s); }
+  __device__ float pvalue() const { return s; }  // block partial, in the partial type
 };
 template <>
 struct Dot<1> {
@@ -94,13 +99,49 @@ struct Dot<1> {
     lo = __fadd_rn(lo, __fadd_rn(err, e));
   }
   __device__ double value() const { return double(hi) + double(lo); }
+  __device__ float2 pvalue() const { return make_float2(hi, lo); }
 };
 template <>
 struct Dot<2> {
   double s = 0.0;
   __device__ void add(double a, double b) { s = __fma_rn(a, b, s); }
   __device__ double value() const { return s; }
+  __device__ double pvalue() const { return s; }
 };
+
+// Type of the hot kernels' block partials: fp32 for FP32 dots, a double-float
+// pair (hi + lo, about 44 significant bits after the two-sum additions) for
+// MIXED, fp64 for FP64.  The FP32 and MIXED sums across threads and CTAs so
+// never touch GB300's narrow FP64 pipe.
+template <int DM>
+using PartT = typename std::conditional<DM == 0, float,
+                                        typename std::conditional<DM == 1, float2, double>::type>::type;
+
+// Addition of block partials (double-float: Knuth's two-sum of the high
+// parts, the low parts added to its error, then a fast two-sum to
+// renormalise; strict fp32 operations).
+__device__ __forceinline__ float padd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double padd(double a, double b) { return a + b; }
+__device__ __forceinline__ float2 padd(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bp = __fsub_rn(s, a.x);
+  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bp)), __fsub_rn(b.x, bp));
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  const float hi = __fadd_rn(s, e);
+  return make_float2(hi, __fsub_rn(e, __fsub_rn(hi, s)));
+}
+template <typename P>
+__device__ __forceinline__ P pzero() { return P(0); }
+template <>
+__device__ __forceinline__ float2 pzero<float2>() { return make_float2(0.f, 0.f); }
+__device__ __forceinline__ double ptod(float v) { return double(v); }
+__device__ __forceinline__ double ptod(double v) { return v; }
+__device__ __forceinline__ double ptod(float2 v) { return double(v.x) + double(v.y); }
+__device__ __forceinline__ float pshfl_down(float v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double pshfl_down(double v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ float2 pshfl_down(float2 v, int o) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, o), __shfl_down_sync(0xffffffffu, v.y, o));
+}
 
 // Block-level sum of NV values.  DM 0 sums in fp32, otherwise fp64.
 // Result valid in thread 0.
@@ -141,6 +182,73 @@ __device__ void block_sum(double (&v)[NV]) {
   __syncthreads();
 }
 
+// Block sum of partial-typed values: warp tree, then thread 0 adds the warp
+// results in order (for float, the order and so the totals of block_sum<0>).
+// Result valid in thread 0.
+template <typename P, int NV, int NT>
+__device__ void block_sum_p(P (&v)[NV]) {
+  __shared__ P sh[NV][NT / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    P x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = padd(x, pshfl_down(x, o));
+    v[k] = x;
+    if (lane == 0) sh[k][w] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      P x = pzero<P>();
+      for (int i = 0; i < NT / 32; ++i) x = padd(x, sh[k][i]);
+      v[k] = x;
+    }
+  }
+}
+
+// Sum of nparts block partials per value (part[k * maxb + b]), in a fixed
+// order: thread t adds partials t, t + NT, ... in batches of 8 independent
+// loads, then the block tree of block_sum.  Every CTA that calls it on the
+// same partials gets the same totals.  Result valid in thread 0.
+template <int DM, int NV, int NT>
+__device__ __forceinline__ void sum_parts(const double* part, int maxb, int nparts,
+                                          double (&acc)[NV]) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const double* pk = part + k * maxb;
+    if (DM == 0) {
+      float x = 0.f;
+      for (int i0 = threadIdx.x; i0 < nparts; i0 += NT * 8) {
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u * NT;
+          t[u] = i < nparts ? float(__ldcg(pk + i)) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x = __fadd_rn(x, t[u]);
+      }
+      acc[k] = double(x);
+    } else {
+      double x = 0.0;
+      for (int i0 = threadIdx.x; i0 < nparts; i0 += NT * 8) {
+        double t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + u * NT;
+          t[u] = i < nparts ? __ldcg(pk + i) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x += t[u];
+      }
+      acc[k] = x;
+    }
+  }
+  block_sum<DM, NV, NT>(acc);
+}
+
 // Single-pass grid reduction: every block deposits its NV partials; the last
 // block to arrive sums them in a fixed order (deterministic) and returns
 // true in all of its threads with the totals in tot (thread 0).
@@ -159,41 +267,8 @@ __device__ bool grid_sum(double (&v)[NV], double* part, int maxb, unsigned int* 
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  // all partials are read in parallel (8 independent loads in flight per
-  // thread), then summed in a fixed order: deterministic
   double acc[NV];
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    const double* pk = part + k * maxb;
-    if (DM == 0) {
-      float x = 0.f;
-      for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += NT * 8) {
-        float t[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int i = i0 + u * NT;
-          t[u] = i < int(gridDim.x) ? float(__ldcg(pk + i)) : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) x = __fadd_rn(x, t[u]);
-      }
-      acc[k] = double(x);
-    } else {
-      double x = 0.0;
-      for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += NT * 8) {
-        double t[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int i = i0 + u * NT;
-          t[u] = i < int(gridDim.x) ? __ldcg(pk + i) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) x += t[u];
-      }
-      acc[k] = x;
-    }
-  }
-  block_sum<DM, NV, NT>(acc);
+  sum_parts<DM, NV, NT>(part, maxb, int(gridDim.x), acc);
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) tot[k] = acc[k];
@@ -220,6 +295,7 @@ struct PcgArgs {
   float* dinner;    // MIXED inner solution (the fp32 x of the inner solve)
   PcgScalars* sc;
   double* part;
+  float* partf;     // fp32 / double-float block partials of the hot kernels (FP32, MIXED)
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
   int par;          // spmv / update: parity of the iteration this launch serves
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
@@ -307,6 +383,17 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
     sc->beta = 0.0;
     if (sc->mode == FSIM_PCG_RELATIVE) sc->thr = sc->tol2 * sc->bb;
     sc->done = (sc->max_iter <= 0) || converged(sc, sc->rr);
+    // the first spmv takes r.r, r.z and beta = 0 from here
+    PcgIterState o;
+    o.rr = sc->rr;
+    o.rz = sc->rz;
+    o.beta = 0.0;
+    o.rz_prev = 0.0;
+    o.iter = 0;
+    o.done = sc->done;
+    o.status = FSIM_OK;
+    o.given = 1;
+    sc->st[1] = o;
   }
 }
 
@@ -536,30 +623,227 @@ __device__ __forceinline__ T pnew_of(const DiagInv<T>* tab, uint8_t f, T r, T po
   return tadd(tmul(tab[f & 15].inv, r), tmul(beta, po));
 }
 
-// Programmatic dependent launch: a kernel launched with a programmatic edge
-// may start while its predecessor finishes.  Everything before pdl_wait()
-// reads only data the predecessor does not write; pdl_wait() returns once
-// the predecessor grid has completed and its writes are visible (at once
-// when there is no programmatic edge).  pdl_trigger() lets the successor
-// start launching.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() {
-  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+// ---- deferred reductions ------------------------------------------------------
+// The hot kernels do not finish their own dot products.  Each CTA writes its
+// block partial and exits; every CTA of the NEXT kernel sums all of them in
+// the same fixed order, so every CTA forms the same alpha or beta,
+// deterministically, and no grid-wide atomic or last-CTA step sits between
+// two launches: kernel order alone makes the partials visible.
+// Partials: update -> spmv (r.r, r.z) at part[0], part[maxb]; spmv -> update
+// (p.Ap) at part[3 * maxb].  The rest of the iteration state goes through
+// PcgScalars::st: each kernel reads its predecessor's slot and CTA 0 writes
+// the other (st[0] spmv -> update, st[1] update -> spmv); the public fields
+// (rr, iter, done, status, ...) are written by CTA 0 for the host.
+//
+// A kernel's head first copies the partial rows and the scalar block into
+// shared memory with cp.async (no registers held), then issues its first half
+// leaf's loads, and only then waits for the copies and sums: the L2 round
+// trip of the head hides under the first loads from HBM.
+constexpr int kPartPAp = 3;       // part[] row of the spmv's p.Ap partials
+constexpr int kMaxHotGrid = 1022; // hot grids stay below this (even) size
+
+struct HotHead {
+  int done;
+  double s;  // beta (spmv) or alpha (update)
+};
+
+template <int NV, typename P>
+struct HeadStage {
+  P part[NV][kMaxHotGrid + 2];
+  PcgScalars sc;
+  HotHead out;
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+template <int DM>
+__device__ __forceinline__ PartT<DM>* part_rows(const PcgArgs& a) {
+  if constexpr (DM == 2) return a.part;
+  else return reinterpret_cast<PartT<DM>*>(a.partf);
+}
+
+// Copies partial rows row0 .. row0+NV-1 of the previous launch (same grid)
+// and the scalar block into hs.  Rows start 16-byte aligned (maxb is a
+// multiple of 4) and a row copy may take up to 3 values past gridDim.x,
+// which lie inside the row and inside hs.part.
+template <int DM, int NV>
+__device__ __forceinline__ void head_issue(HeadStage<NV, PartT<DM>>& hs, const PcgArgs& a,
+                                           int row0) {
+  constexpr int per = 16 / int(sizeof(PartT<DM>));
+  const int nch = (int(gridDim.x) + per - 1) / per;  // 16-byte chunks per row
+  const PartT<DM>* rows = part_rows<DM>(a);
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+    for (int c = threadIdx.x; c < nch; c += kHotThreads)
+      cp_async16(&hs.part[k][per * c], rows + int64_t(row0 + k) * a.maxb + per * c);
+  constexpr int nsc = int(sizeof(PcgScalars)) / 16;
+  for (int c = threadIdx.x; c < nsc; c += kHotThreads)
+    cp_async16(reinterpret_cast<char*>(&hs.sc) + 16 * c,
+               reinterpret_cast<const char*>(a.sc) + 16 * c);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// Waits for the copies and sums each row in the order of sum_parts (thread t
+// adds partials t, t + 128, ...; then the block tree).  Result valid in
+// thread 0.
+template <int DM, int NV>
+__device__ __forceinline__ void head_sum(HeadStage<NV, PartT<DM>>& hs, double (&acc)[NV]) {
+  using P = PartT<DM>;
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncthreads();
+  const int nparts = int(gridDim.x);
+  P x[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    x[k] = pzero<P>();
+    for (int i = threadIdx.x; i < nparts; i += kHotThreads) x[k] = padd(x[k], hs.part[k][i]);
+  }
+  block_sum_p<P, NV, kHotThreads>(x);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) acc[k] = ptod(x[k]);  // thread 0 uses them
+}
+
+// Head of the spmv of iteration j: r.r, r.z of the previous update (summed
+// from its partials, or given by setup / residual replacement), beta =
+// r.z / r.z_old with ComputeLocal3's CHECK_LE(beta, LARGE_FLOAT), then the
+// loop test of PCGDriver::Solve (iterations >= max, or converged).
+template <int DM>
+__device__ __forceinline__ HotHead spmv_head(HeadStage<2, PartT<DM>>& hs, const PcgArgs& a) {
+  double acc[2];
+  head_sum<DM, 2>(hs, acc);
+  if (threadIdx.x == 0) {
+    const PcgScalars* cs = &hs.sc;  // the scalar block as the previous launch left it
+    const PcgIterState in = cs->st[1];
+    double rr, rz, beta;
+    if (in.given) {
+      rr = in.rr;
+      rz = in.rz;
+      beta = in.beta;
+    } else {
+      rr = round_t(cs, acc[0]);
+      rz = round_t(cs, acc[1]);
+      beta = cs->fp32 ? double(__fdiv_rn(float(rz), float(in.rz_prev))) : rz / in.rz_prev;
+    }
+    int done = in.done, status = in.status;
+    if (!done) {
+      if (!in.given && !(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
+        status = FSIM_ERR_BREAKDOWN;
+        done = 1;
+      } else {
+        done = (in.iter >= cs->max_iter) || converged(cs, rr);
+      }
+    }
+    if (blockIdx.x == 0) {
+      PcgScalars* sc = a.sc;
+      if (in.done) {
+        sc->st[0].done = 1;  // nothing new: pass the stop flag on
+      } else {
+        PcgIterState o = in;
+        o.rr = rr;
+        o.rz = rz;
+        o.beta = beta;
+        o.done = done;
+        o.status = status;
+        o.given = 0;
+        sc->st[0] = o;
+        sc->rr = rr;
+        sc->rz = rz;
+        sc->rz_old = in.rz_prev;
+        sc->beta = beta;
+        sc->iter = in.iter;
+        sc->status = status;
+        sc->done = done;
+      }
+      if (done && a.cond) cudaGraphSetConditional(a.cond, 0u);  // ends the WHILE loop
+    }
+    hs.out.done = done;
+    hs.out.s = beta;
+  }
+  __syncthreads();
+  return hs.out;
+}
+
+// Head of the update of iteration j: p.Ap summed from the spmv's partials,
+// alpha = r.z / p.Ap with ComputeLocal2's CHECK_LE(alpha, LARGE_FLOAT).
+template <int DM>
+__device__ __forceinline__ HotHead update_head(HeadStage<1, PartT<DM>>& hs, const PcgArgs& a) {
+  double acc[1];
+  head_sum<DM, 1>(hs, acc);
+  if (threadIdx.x == 0) {
+    const PcgScalars* cs = &hs.sc;
+    const PcgIterState in = cs->st[0];
+    int done = in.done, status = in.status;
+    double alpha = 0.0, pAp = 0.0;
+    if (!done) {
+      pAp = round_t(cs, acc[0]);
+      alpha = cs->fp32 ? double(__fdiv_rn(float(in.rz), float(pAp))) : in.rz / pAp;
+      if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
+        status = FSIM_ERR_BREAKDOWN;
+        done = 1;
+      }
+    }
+    if (blockIdx.x == 0) {
+      PcgScalars* sc = a.sc;
+      if (in.done) {
+        sc->st[1].done = 1;
+      } else {
+        sc->pAp = pAp;
+        sc->alpha = alpha;
+        if (done) {
+          sc->st[1].done = 1;
+          sc->st[1].status = status;
+          sc->status = status;
+          sc->done = 1;
+        } else {
+          PcgIterState o;
+          o.rr = 0.0;
+          o.rz = 0.0;
+          o.beta = 0.0;
+          o.rz_prev = in.rz;
+          o.iter = in.iter + 1;
+          o.done = 0;
+          o.status = status;
+          o.given = 0;
+          sc->st[1] = o;
+          sc->iter = in.iter + 1;
+        }
+      }
+      if (done && a.cond) cudaGraphSetConditional(a.cond, 0u);
+    }
+    hs.out.done = done;
+    hs.out.s = alpha;
+  }
+  __syncthreads();
+  return hs.out;
+}
+
+// This CTA's share of a dot product, for the next kernel's head.
+template <int DM, int NV>
+__device__ __forceinline__ void put_partials(const PcgArgs& a, int row0, PartT<DM> (&v)[NV]) {
+  block_sum_p<PartT<DM>, NV, kHotThreads>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) part_rows<DM>(a)[(row0 + k) * a.maxb + blockIdx.x] = v[k];
+  }
 }
 
 // Each launch of the hot kernels serves one iteration of known parity
-// (PcgArgs::par), so its buffers are fixed before the device scalars are
-// read: the first half leaf's own-column loads are issued together with the
-// loads of the stop flag and the step scalars.
+// (PcgArgs::par), so its buffers are fixed before the scalars are known: the
+// first half leaf's own-column loads are issued before the head sums the
+// previous kernel's partials.
 //
 // p_j = z_j + beta_{j-1} p_{j-1} on the half leaf and its halo (z = r/diag
-// recomputed, never stored), then p_j.(A p_j); the last CTA forms alpha_j.
-// Only p_j is written: the update kernel recomputes A p_j from it.
+// recomputed, never stored), then this CTA's part of p_j.(A p_j).  Only p_j
+// is written: the update kernel recomputes A p_j from it.
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_spmv(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<2, PartT<DM>> hs;
   const int par = a.par;
   const T* r = static_cast<const T*>(a.r);
   const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
@@ -569,25 +853,21 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  // first half leaf: flags, p_{j-1} (written two launches back) and face
-  // slots before the wait; r and the scalars (written by the previous
-  // update) after it
+  head_issue<DM, 2>(hs, a, 0);
+  // first half leaf: flags, p_{j-1}, r and the face slots
   Col<T> rc, pc;
   uint2 f = make_uint2(0u, 0u);
   const int64_t o0 = hw < nhw ? int64_t(hw >> 1) * 512 + half_pos(hw, lane).c : 0;
   if (hw < nhw) {
     f = ldflags(a.flags, o0);
     ldcol(pold, o0, pc);
+    ldcol(r, o0, rc);
   }
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
   fill_diag_table<T>(tab);
-  pdl_wait();
-  const PcgScalars* sc = a.sc;
-  const int done = sc->done;
-  const T beta = T(sc->beta);
-  if (hw < nhw) ldcol(r, o0, rc);
-  __syncthreads();
-  if (done) return;
+  const HotHead head = spmv_head<DM>(hs, a);
+  if (head.done) return;
+  const T beta = T(head.s);
   Tile<T>& tile = tiles[threadIdx.x >> 5];
   Dot<DM> dp;
   for (; hw < nhw; hw += hstride) {
@@ -657,28 +937,18 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
 #pragma unroll
     for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
   }
-  pdl_trigger();
-  double v[1] = {dp.value()};
-  double tot[1];
-  if (grid_sum<DM, 1, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
-    PcgScalars* s = a.sc;
-    s->pAp = round_t(s, tot[0]);
-    double alpha = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->pAp))) : s->rz / s->pAp;
-    s->alpha = alpha;
-    if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
-      s->status = FSIM_ERR_BREAKDOWN;
-      s->done = 1;
-    }
-  }
+  PartT<DM> v[1] = {dp.pvalue()};
+  put_partials<DM, 1>(a, kPartPAp, v);
 }
 
 // A p_j recomputed from p_j (half leaf + halo); x += alpha p;
-// r -= alpha Ap; r.r and r.z; the last CTA forms beta and the stop test.
+// r -= alpha Ap; this CTA's parts of r.r and r.z.
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_update(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<1, PartT<DM>> hs;
   const int par = a.par;
   const T* p = static_cast<const T*>(par ? a.p1 : a.p0);
   T* x = static_cast<T*>(a.x);
@@ -688,8 +958,8 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  // first half leaf: flags, x, r (not written by the spmv) and face slots
-  // before the wait; p_j and the scalars after it
+  head_issue<DM, 1>(hs, a, kPartPAp);
+  // first half leaf: flags, x, r, p_j and the face slots
   Col<T> P, xc, rc;
   uint2 f = make_uint2(0u, 0u);
   const int64_t o0 = hw < nhw ? int64_t(hw >> 1) * 512 + half_pos(hw, lane).c : 0;
@@ -697,22 +967,13 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     f = ldflags(a.flags, o0);
     ldcol(x, o0, xc);
     ldcol(r, o0, rc);
+    ldcol(p, o0, P);
   }
   int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
   fill_diag_table<T>(tab);
-  pdl_wait();
-  const PcgScalars* sc = a.sc;
-  const int done = sc->done;
-  const int it = sc->iter;
-  const T alpha = T(sc->alpha);
-  if (hw < nhw) ldcol(p, o0, P);
-  __syncthreads();
-  if (done) {
-    // stop flag already set (converged at setup, or breakdown in spmv):
-    // end the graph's WHILE loop
-    if (a.cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
-    return;
-  }
+  const HotHead head = update_head<DM>(hs, a);
+  if (head.done) return;
+  const T alpha = T(head.s);
   const T nalpha = -alpha;
   Tile<T>& tile = tiles[threadIdx.x >> 5];
   Dot<DM> drr, drz;
@@ -769,25 +1030,8 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
       ldcol(r, on, rc);
     }
   }
-  pdl_trigger();
-  double v[2] = {drr.value(), drz.value()};
-  double tot[2];
-  if (grid_sum<DM, 2, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
-    PcgScalars* s = a.sc;
-    s->rr = round_t(s, tot[0]);
-    s->rz_old = s->rz;
-    s->rz = round_t(s, tot[1]);
-    double beta = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->rz_old))) : s->rz / s->rz_old;
-    s->beta = beta;
-    s->iter = it + 1;
-    if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
-      s->status = FSIM_ERR_BREAKDOWN;
-      s->done = 1;
-    } else {
-      s->done = (s->iter >= s->max_iter) || converged(s, s->rr);
-    }
-    if (a.cond) cudaGraphSetConditional(a.cond, s->done ? 0u : 1u);
-  }
+  PartT<DM> v[2] = {drr.pvalue(), drz.pvalue()};
+  put_partials<DM, 2>(a, 0, v);
 }
 
 // ---- register-pipelined variants --------------------------------------------
@@ -803,14 +1047,23 @@ struct SpmvIn {
   T zr0, zr1, zq0, zq1;
 };
 
+// The own column (independent of the neighbour table) ...
 template <typename T>
-__device__ __forceinline__ void spmv_load(const PcgArgs& a, int hw, int lane, const int fs[6],
-                                          const T* r, const T* pold, int qold, SpmvIn<T>& in) {
+__device__ __forceinline__ void spmv_load_own(const PcgArgs& a, int hw, int lane, const T* r,
+                                              const T* pold, SpmvIn<T>& in) {
   const HalfLeaf h = half_pos(hw, lane);
   const int64_t o = int64_t(h.s) * 512 + h.c;
   in.f = ldflags(a.flags, o);
   ldcol(r, o, in.rc);
   ldcol(pold, o, in.pc);
+}
+
+// ... and the halo column and z faces, addressed through the face slots.
+template <typename T>
+__device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lane, const int fs[6],
+                                               const T* r, const T* pold, int qold,
+                                               SpmvIn<T>& in) {
+  const HalfLeaf h = half_pos(hw, lane);
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
   const bool hv = hslot >= 0 && hslot < a.n_pleaf;
@@ -837,10 +1090,18 @@ __device__ __forceinline__ void spmv_load(const PcgArgs& a, int hw, int lane, co
   in.zq1 = zv1 ? ldv(zf + zo1 + 128 * qold) : T(0);
 }
 
+template <typename T>
+__device__ __forceinline__ void spmv_load(const PcgArgs& a, int hw, int lane, const int fs[6],
+                                          const T* r, const T* pold, int qold, SpmvIn<T>& in) {
+  spmv_load_own<T>(a, hw, lane, r, pold, in);
+  spmv_load_halo<T>(a, hw, lane, fs, r, pold, qold, in);
+}
+
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<2, PartT<DM>> hs;
   const int par = a.par;
   const T* r = static_cast<const T*>(a.r);
   const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
@@ -850,20 +1111,22 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  head_issue<DM, 2>(hs, a, 0);
   fill_diag_table<T>(tab);
-  const PcgScalars* sc = a.sc;
-  const int done = sc->done;
-  const T beta = T(sc->beta);
   SpmvIn<T> cur;
   int nbl = -1;
   if (hw < nhw) {
-    int fs[6];
-    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
-    spmv_load<T>(a, hw, lane, fs, r, pold, qold, cur);
+    // own column first: its loads fly while the face slots arrive
+    const int nb0 = face_slot_lane(a.nbr, hw >> 1, lane);
+    spmv_load_own<T>(a, hw, lane, r, pold, cur);
     nbl = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+    int fs[6];
+    face_slots(nb0, fs);
+    spmv_load_halo<T>(a, hw, lane, fs, r, pold, qold, cur);
   }
-  __syncthreads();
-  if (done) return;
+  const HotHead head = spmv_head<DM>(hs, a);
+  if (head.done) return;
+  const T beta = T(head.s);
   Tile<T>& tile = tiles[threadIdx.x >> 5];
   Dot<DM> dp;
   while (hw < nhw) {
@@ -902,18 +1165,8 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
     cur = nxt;
     hw = hn;
   }
-  double v[1] = {dp.value()};
-  double tot[1];
-  if (grid_sum<DM, 1, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_a, tot) && threadIdx.x == 0) {
-    PcgScalars* s = a.sc;
-    s->pAp = round_t(s, tot[0]);
-    double alpha = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->pAp))) : s->rz / s->pAp;
-    s->alpha = alpha;
-    if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
-      s->status = FSIM_ERR_BREAKDOWN;
-      s->done = 1;
-    }
-  }
+  PartT<DM> v[1] = {dp.pvalue()};
+  put_partials<DM, 1>(a, kPartPAp, v);
 }
 
 template <typename T>
@@ -924,15 +1177,20 @@ struct UpdIn {
 };
 
 template <typename T>
-__device__ __forceinline__ void upd_load(const PcgArgs& a, int hw, int lane, const int fs[6],
-                                         const T* p, const T* x, const T* r, int qcur,
-                                         UpdIn<T>& in) {
+__device__ __forceinline__ void upd_load_own(const PcgArgs& a, int hw, int lane, const T* p,
+                                             const T* x, const T* r, UpdIn<T>& in) {
   const HalfLeaf h = half_pos(hw, lane);
   const int64_t o = int64_t(h.s) * 512 + h.c;
   in.f = ldflags(a.flags, o);
   ldcol(p, o, in.P);
   ldcol(x, o, in.x);
   ldcol(r, o, in.r);
+}
+
+template <typename T>
+__device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane, const int fs[6],
+                                              const T* p, int qcur, UpdIn<T>& in) {
+  const HalfLeaf h = half_pos(hw, lane);
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
   if (hslot >= 0 && hslot < a.n_pleaf) {
@@ -947,11 +1205,20 @@ __device__ __forceinline__ void upd_load(const PcgArgs& a, int hw, int lane, con
   in.zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + int64_t(zs1) * 384) : T(0);
 }
 
+template <typename T>
+__device__ __forceinline__ void upd_load(const PcgArgs& a, int hw, int lane, const int fs[6],
+                                         const T* p, const T* x, const T* r, int qcur,
+                                         UpdIn<T>& in) {
+  upd_load_own<T>(a, hw, lane, p, x, r, in);
+  upd_load_halo<T>(a, hw, lane, fs, p, qcur, in);
+}
+
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, 4)
     k_pcg_update_pl(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<1, PartT<DM>> hs;
   const int par = a.par;
   const T* p = static_cast<const T*>(par ? a.p1 : a.p0);
   T* x = static_cast<T*>(a.x);
@@ -961,24 +1228,21 @@ __global__ void __launch_bounds__(kHotThreads, 4)
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  head_issue<DM, 1>(hs, a, kPartPAp);
   fill_diag_table<T>(tab);
-  const PcgScalars* sc = a.sc;
-  const int done = sc->done;
-  const int it = sc->iter;
-  const T alpha = T(sc->alpha);
   UpdIn<T> cur;
   int nbl = -1;
   if (hw < nhw) {
-    int fs[6];
-    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
-    upd_load<T>(a, hw, lane, fs, p, x, r, qcur, cur);
+    const int nb0 = face_slot_lane(a.nbr, hw >> 1, lane);
+    upd_load_own<T>(a, hw, lane, p, x, r, cur);
     nbl = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+    int fs[6];
+    face_slots(nb0, fs);
+    upd_load_halo<T>(a, hw, lane, fs, p, qcur, cur);
   }
-  __syncthreads();
-  if (done) {
-    if (a.cond && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.cond, 0u);
-    return;
-  }
+  const HotHead head = update_head<DM>(hs, a);
+  if (head.done) return;
+  const T alpha = T(head.s);
   const T nalpha = -alpha;
   Tile<T>& tile = tiles[threadIdx.x >> 5];
   Dot<DM> drr, drz;
@@ -1017,24 +1281,8 @@ __global__ void __launch_bounds__(kHotThreads, 4)
     cur = nxt;
     hw = hn;
   }
-  double v[2] = {drr.value(), drz.value()};
-  double tot[2];
-  if (grid_sum<DM, 2, kHotThreads>(v, a.part, a.maxb, &a.sc->cnt_b, tot) && threadIdx.x == 0) {
-    PcgScalars* s = a.sc;
-    s->rr = round_t(s, tot[0]);
-    s->rz_old = s->rz;
-    s->rz = round_t(s, tot[1]);
-    double beta = s->fp32 ? double(__fdiv_rn(float(s->rz), float(s->rz_old))) : s->rz / s->rz_old;
-    s->beta = beta;
-    s->iter = it + 1;
-    if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
-      s->status = FSIM_ERR_BREAKDOWN;
-      s->done = 1;
-    } else {
-      s->done = (s->iter >= s->max_iter) || converged(s, s->rr);
-    }
-    if (a.cond) cudaGraphSetConditional(a.cond, s->done ? 0u : 1u);
-  }
+  PartT<DM> v[2] = {drr.pvalue(), drz.pvalue()};
+  put_partials<DM, 2>(a, 0, v);
 }
 
 // ---- persistent PCG loop (cooperative launch) ------------------------------
@@ -1407,6 +1655,17 @@ __global__ void __launch_bounds__(kThreads) k_pcg_replace(const __grid_constant_
     sc->thr = fmax(sc->tol2 * tot[0], sc->tol2_outer * sc->bb);
     sc->status = FSIM_OK;
     sc->done = (sc->iter >= sc->max_iter) ? 1 : 0;
+    // the resuming spmv takes r'.r', r'.z' and beta from here
+    PcgIterState o;
+    o.rr = sc->rr;
+    o.rz = sc->rz;
+    o.beta = sc->beta;
+    o.rz_prev = sc->rz_old;
+    o.iter = sc->iter;
+    o.done = sc->done;
+    o.status = FSIM_OK;
+    o.given = 1;
+    sc->st[1] = o;
   }
 }
 
@@ -1420,15 +1679,15 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
 // Builds and launches graph = WHILE(cond){ (spmv; update) x kPassIters } on
 // the handle's stream: one pass runs kPassIters iterations of alternating
 // parity (their buffers are fixed by PcgArgs::par), and kernels launched
-// after the stop flag is set return at once.  With pdl the kernels of a
-// pass are joined by programmatic edges, so each one's prologue overlaps
-// its predecessor's reduction tail.  Returns FSIM_OK, or FSIM_ERR_CUDA when the graph API refuses
-// (the caller then polls from the host).  Kernel launches inside the graph
-// are counted by the caller from the iteration count the solve reports.
+// after the stop flag is set return at once.  The head of the kernel that
+// sets the stop flag clears the condition.  Returns FSIM_OK, or
+// FSIM_ERR_CUDA when the graph API refuses (the caller then polls from the
+// host).  Kernel launches inside the graph are counted by the caller from
+// the iteration count the solve reports.
 constexpr int kPassIters = 4;  // PCG iterations per pass of the graph's WHILE body
 
 template <typename T, int DM>
-int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl, int par0) {
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -1461,14 +1720,8 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl, int par0) {
       else
         kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
                                  : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
-      cudaGraphEdgeData ed = {};
-      if (pdl) {
-        ed.from_port = cudaGraphKernelNodePortProgrammatic;
-        ed.type = cudaGraphDependencyTypeProgrammatic;
-      }
       cudaGraphNode_t n = nullptr;
-      e = cudaGraphAddNode(&n, body, prev ? &prev : nullptr, prev ? &ed : nullptr, prev ? 1 : 0,
-                           &kn);
+      e = cudaGraphAddNode(&n, body, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &kn);
       prev = n;
     }
   }
@@ -1484,9 +1737,9 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, bool pdl, int par0) {
 }
 
 // One inner solve: setup, then the iterations.  The iterations run as a CUDA
-// graph whose conditional WHILE node repeats {spmv, update}; the update
-// kernel's last CTA clears the condition when the stop flag is set, so the
-// whole loop runs without a host round trip.  The loop is bounded by the
+// graph whose conditional WHILE node repeats {spmv, update}; the kernel head
+// that sets the stop flag clears the condition, so the whole loop runs
+// without a host round trip.  The loop is bounded by the
 // solve's max_iterations (the stop flag is set at that count).  If graph
 // construction is not available the host launches chunks of iterations and
 // polls the stop flag between them (kernels launched after it is set return
@@ -1507,7 +1760,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   }
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
-                                          s->max_blocks}));
+                                          s->max_blocks, kMaxHotGrid}));
   if (s->use_coop && !s->profiling) {
     // one cooperative launch runs every iteration (setup has already run)
     int occ = 0;
@@ -1537,20 +1790,16 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   }
   const int it0 = setup ? 0 : s->h_sc->iter;  // iterations before this segment
   if (s->use_graphs && !s->profiling) {
-    int rc = FSIM_ERR_CUDA;
-    if (s->use_pdl) {
-      rc = run_graph_loop<T, DM>(s, a, wgrid, true, par0);
-      if (rc != FSIM_OK) s->use_pdl = false;  // programmatic edges refused: plain edges
-    }
-    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, false, par0);
+    const int rc = run_graph_loop<T, DM>(s, a, wgrid, par0);
     if (rc == FSIM_OK) {
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
-      // each WHILE pass runs two iterations (four kernels); the pass that
-      // sees the stop flag at setup or after a breakdown also counts
-      const int64_t pairs = std::max(s->h_sc->iter - it0 + (s->h_sc->status ? 1 : 0), 1);
-      s->launches += 2 * kPassIters * ((pairs + kPassIters - 1) / kPassIters);
+      // each WHILE pass launches 2 * kPassIters kernels; the stop flag is
+      // set in the head of iteration n (n = iterations completed here), so
+      // n / kPassIters + 1 passes ran
+      const int64_t n = std::max(s->h_sc->iter - it0, 0);
+      s->launches += 2 * kPassIters * (n / kPassIters + 1);
       return FSIM_OK;
     }
     s->use_graphs = false;  // fall back for the rest of this handle's life
@@ -1611,6 +1860,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
   a.flags = s->flags;
   a.sc = s->d_sc;
   a.part = s->d_part;
+  a.partf = s->d_partf;
   a.zf = s->zface;
   a.zff = s->zflags;
   a.p0 = s->p[0];

@@ -97,6 +97,34 @@ def test_mixed_segments_stop_at_the_outer_target():
     sim.close()
 
 
+def test_loop_variants_agree(monkeypatch):
+    """The graph loop, host polling and the unpipelined kernels run the same
+    arithmetic in the same order (bitwise equal solves); the cooperative
+    persistent loop sums its partials over its own grid (equal to 1e-5)."""
+    variants = (("graph", {}), ("host", {"FSIM_PCG_GRAPH": "0"}),
+                ("unpiped", {"FSIM_PCG_PIPE": "0"}), ("coop", {"FSIM_PCG_COOP": "1"}))
+    solves = ((fsim.PREC_FP32, 1e-5), (fsim.PREC_MIXED, 1e-7), (fsim.PREC_FP64, 1e-7))
+    got = {}
+    for name, env in variants:
+        with monkeypatch.context() as m:
+            for k, v in env.items():
+                m.setenv(k, v)
+            orc, sim = _prepared()
+            for prec, tol in solves:
+                st = sim.pcg_solve(fsim.pcg_params(fsim.PCG_RELATIVE, prec, 3000, tolerance=tol,
+                                                   max_refinements=20))
+                assert st.status == 0, (name, prec)
+                got[name, prec] = (st.iterations, st.rr, sim.field(fsim.FIELD_PRESSURE)[0])
+            sim.close()
+    for prec, _ in solves:
+        it, rr, x = got["graph", prec]
+        for name in ("host", "unpiped"):
+            it2, rr2, x2 = got[name, prec]
+            assert it2 == it and rr2 == rr and np.array_equal(x2, x), (name, prec)
+        it2, rr2, x2 = got["coop", prec]
+        assert abs(it2 - it) <= 2 and rel_l2(x2, x) <= 1e-5, prec
+
+
 def test_fp64_matches_fp64_oracle():
     orc, sim = _prepared(n=24, scene="sphere_drop")
     ost = orc.pcg_solve(mode=1, precision=2, max_iterations=20000, tol=1e-12)
