@@ -241,6 +241,7 @@ def run_gpu(args, rank, world):
     e1 = torch.cuda.Event(enable_timing=True)
     marks = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(e2e_steps)]
     e0.record(stream)
+    # (a) the three calls in sequence: upload, step, download (for the split)
     for k in range(e2e_steps):
         marks[k][0].record(stream)
         rc = sim.lib.fsim_upload_particles(sim.h, hp.data_ptr(), hv.data_ptr(), hg.data_ptr(),
@@ -262,9 +263,23 @@ def run_gpu(args, rank, world):
             hp, hv, hg = hp[:cnt], hv[:cnt], hg[:cnt]
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    seq_ms = e0.elapsed_time(e1) / e2e_steps
     e2e_split = {name: sum(m[i].elapsed_time(m[i + 1]) for m in marks) / e2e_steps
                  for i, name in enumerate(("upload_ms", "step_ms", "download_ms"))}
+    # (b) the headline: fsim_step_host, one call per step with the copies
+    # overlapping the step (in place on the same pinned buffers)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(e2e_steps):
+        st, cnt = sim.step_host(next_dt(), prm, hp, hv, hg, out=(hp, hv, hg))
+        inv = st.next_inv_speed
+        if cnt < hp.shape[0]:
+            hp, hv, hg = hp[:cnt], hv[:cnt], hg[:cnt]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_split["sequential_calls_ms"] = seq_ms
     barrier()
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], device=f"cuda:{device}")
     sim.close()

@@ -306,6 +306,13 @@ int fsim_destroy(fsim_t* s) {
   if (s->h_sc) cudaFreeHost(s->h_sc);
   for (auto& p : s->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto e : s->ev_pool) cudaEventDestroy(e);
+  if (s->io_stream) {
+    cudaStreamSynchronize(s->io_stream);
+    cudaStreamDestroy(s->io_stream);
+  }
+  if (s->ev_main) cudaEventDestroy(s->ev_main);
+  if (s->ev_io) cudaEventDestroy(s->ev_io);
+  dfree(s->io_stage);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return FSIM_OK;
@@ -641,6 +648,137 @@ int fsim_update_particles_from_grid(fsim_t* s) {
   return launch_g2p(s);
 }
 
+namespace {
+
+// fsim_step_host: the positions are final once the step has sorted and
+// gathered the particles (G2P changes only vel and gvel), so they are
+// converted to AoS and copied to the host on the I/O stream while the rest
+// of the step runs.
+int start_early_position_download(fsim_sim* s) {
+  const int64_t nl = s->n_live;
+  s->io_early_n = -1;
+  if (nl > s->io_early_cap || nl == 0) return FSIM_OK;  // the final download handles it
+  if (s->io_stage_cap < s->cap_p) {
+    dfree(s->io_stage);
+    int rc = dmalloc(s, &s->io_stage, size_t(s->cap_p) * 3);
+    if (rc) return rc;
+    s->io_stage_cap = s->cap_p;
+  }
+  FSIM_CK(s, cudaEventRecord(s->ev_main, s->stream));
+  FSIM_CK(s, cudaStreamWaitEvent(s->io_stream, s->ev_main, 0));
+  k_soa_to_aos<<<unsigned((nl + 255) / 256), 256, 0, s->io_stream>>>(s->part[s->cur], s->io_stage,
+                                                                     nl, s->cap_p, 0);
+  s->launches++;
+  FSIM_CK(s, cudaGetLastError());
+  FSIM_CK(s, cudaMemcpyAsync(s->io_early_pos, s->io_stage, size_t(nl) * 12, cudaMemcpyDeviceToHost,
+                             s->io_stream));
+  s->io_early_n = nl;
+  return FSIM_OK;
+}
+
+int ensure_io_stream(fsim_sim* s) {
+  if (s->io_stream) return FSIM_OK;
+  FSIM_CK(s, cudaStreamCreateWithFlags(&s->io_stream, cudaStreamNonBlocking));
+  FSIM_CK(s, cudaEventCreateWithFlags(&s->ev_main, cudaEventDisableTiming));
+  FSIM_CK(s, cudaEventCreateWithFlags(&s->ev_io, cudaEventDisableTiming));
+  return FSIM_OK;
+}
+
+// Upload with the velocity copy on the I/O stream: positions and PIC
+// velocities (which the rebinning and the advection read) go first on the
+// handle's stream; the velocity lands while they are binned and sorted, and
+// the particle gather waits for it.
+int upload_overlapped(fsim_sim* s, const float* pos, const float* vel, const float* gvel,
+                      int64_t n) {
+  int rc;
+  s->n_total = 0;
+  s->n_live = 0;
+  if ((rc = ensure_particle_capacity(s, n))) return rc;
+  float* stage = s->part[s->cur ^ 1];
+  if (n > 0) {
+    FSIM_CK(s, cudaEventRecord(s->ev_main, s->stream));
+    FSIM_CK(s, cudaStreamWaitEvent(s->io_stream, s->ev_main, 0));
+    for (int f = 0; f < 3; f += 2) {  // pos, gvel
+      const float* src = f == 0 ? pos : gvel;
+      FSIM_CK(s, cudaMemcpyAsync(stage + size_t(f) * 3 * s->cap_p, src, size_t(n) * 12,
+                                 cudaMemcpyHostToDevice, s->stream));
+      FSIM_LAUNCH(s, "aos_to_soa", k_aos_to_soa, unsigned((n + 255) / 256), 256, 0,
+                  stage + size_t(f) * 3 * s->cap_p, s->part[s->cur], n, s->cap_p, 3 * f);
+    }
+    FSIM_CK(s, cudaMemcpyAsync(stage + size_t(3) * s->cap_p, vel, size_t(n) * 12,
+                               cudaMemcpyHostToDevice, s->io_stream));
+    k_aos_to_soa<<<unsigned((n + 255) / 256), 256, 0, s->io_stream>>>(
+        stage + size_t(3) * s->cap_p, s->part[s->cur], n, s->cap_p, 3);
+    s->launches++;
+    FSIM_CK(s, cudaGetLastError());
+    FSIM_CK(s, cudaEventRecord(s->ev_io, s->io_stream));
+    s->io_vel_pending = true;
+  }
+  s->n_total = n;
+  if ((rc = launch_keys_from_positions(s, 0, 0.f))) return rc;
+  int64_t invalid = 0;
+  if ((rc = rebin_uploaded(s, &invalid))) return rc;
+  if (invalid != 0) {
+    s->n_total = 0;
+    s->have_topology = false;
+    return fail(s, FSIM_ERR_INVALID, "particle positions must lie in [0, N] per axis");
+  }
+  return after_sort(s);
+}
+
+}  // namespace
+
+int fsim_step_host(fsim_t* s, float dt, const fsim_pcg_params* prm, const float* pos,
+                   const float* vel, const float* gvel, int64_t n, float* out_pos, float* out_vel,
+                   float* out_gvel, int64_t capacity, int64_t* n_out, fsim_step_stats* st) {
+  if (!s || !prm || !n_out || n < 0 || (n > 0 && (!pos || !vel || !gvel)))
+    return FSIM_ERR_INVALID;
+  cudaSetDevice(s->dev);
+  // the overlapped path needs the particle buffers fixed during the step and
+  // no deletion after the sort: no sources, no tank boundary
+  const bool overlap = s->sources.empty() && s->cfg.boundary != FSIM_BOUNDARY_TANK;
+  int rc = FSIM_OK;
+  if (!overlap) {
+    if ((rc = fsim_upload_particles(s, pos, vel, gvel, n))) return rc;
+    if ((rc = fsim_step(s, dt, prm, st))) return rc;
+    return fsim_download_particles(s, out_pos, out_vel, out_gvel, capacity, n_out);
+  }
+  if ((rc = ensure_io_stream(s))) return rc;
+  rc = upload_overlapped(s, pos, vel, gvel, n);
+  if (rc == FSIM_OK) {
+    s->io_early_pos = out_pos;
+    s->io_early_cap = capacity;
+    s->io_early_n = -1;
+    rc = fsim_step(s, dt, prm, st);
+    s->io_early_pos = nullptr;
+  }
+  if (rc != FSIM_OK) {
+    cudaStreamSynchronize(s->io_stream);
+    s->io_vel_pending = false;
+    return rc;
+  }
+  // velocities after G2P; positions unless the early copy took them
+  const int64_t nl = s->n_live;
+  *n_out = nl;
+  if (nl > capacity) {
+    cudaStreamSynchronize(s->io_stream);
+    return fail(s, FSIM_ERR_CAPACITY, "download capacity too small");
+  }
+  float* stage = s->part[s->cur ^ 1];
+  float* outs[3] = {s->io_early_n == nl ? nullptr : out_pos, out_vel, out_gvel};
+  for (int f = 0; f < 3 && nl > 0; ++f) {
+    if (!outs[f]) continue;
+    float* sg = stage + size_t(f) * 3 * s->cap_p;
+    FSIM_LAUNCH(s, "soa_to_aos", k_soa_to_aos, unsigned((nl + 255) / 256), 256, 0,
+                s->part[s->cur], sg, nl, s->cap_p, 3 * f);
+    FSIM_CK(s, cudaMemcpyAsync(outs[f], sg, size_t(nl) * 12, cudaMemcpyDeviceToHost, s->stream));
+  }
+  FSIM_CK(s, cudaStreamSynchronize(s->stream));
+  FSIM_CK(s, cudaStreamSynchronize(s->io_stream));
+  s->io_early_n = -1;
+  return FSIM_OK;
+}
+
 int fsim_step(fsim_t* s, float dt, const fsim_pcg_params* prm, fsim_step_stats* st) {
   if (!s || !prm) return FSIM_ERR_INVALID;
   int rc = need_topology(s);
@@ -656,6 +794,7 @@ int fsim_step(fsim_t* s, float dt, const fsim_pcg_params* prm, fsim_step_stats* 
   // MoveParticles + DeleteParticlesInSolids
   if ((rc = launch_keys_from_positions(s, 1, dt))) return rc;
   if ((rc = rebuild_topology(s))) return rc;
+  if (s->io_early_pos && (rc = start_early_position_download(s))) return rc;
   reset_grid_flags(s);
   // TransferParticlesToGrid + BC + SaveGridVelocities + AddGravity + BC
   if ((rc = launch_p2g(s, true, dt))) return rc;

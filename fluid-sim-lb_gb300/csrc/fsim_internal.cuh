@@ -187,6 +187,15 @@ struct fsim_sim {
   int dev = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  // fsim_step_host: a second stream for the copies that overlap the step
+  cudaStream_t io_stream = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_io = nullptr;
+  float* io_stage = nullptr;   // AoS staging of the early position download
+  int64_t io_stage_cap = 0;
+  bool io_vel_pending = false; // vel upload in flight on io_stream (ev_io)
+  float* io_early_pos = nullptr;  // host destination of the early position download
+  int64_t io_early_cap = 0;
+  int64_t io_early_n = -1;     // particles the early download copied (-1: none)
   std::string err;
   int64_t launches = 0;
 

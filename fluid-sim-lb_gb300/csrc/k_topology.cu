@@ -530,6 +530,11 @@ int rebuild_after_sort(fsim_sim* s, bool gather) {
   FSIM_CK(s, cudaMemsetAsync(s->d_cnt, 0, 3 * sizeof(int64_t), s->stream));
   FSIM_LAUNCH(s, "count_live", k_count_live, nblk(n, 256), 256, 0, s->keys[0], n, s->d_cnt);
   if (gather) {
+    // a velocity upload still in flight on the I/O stream (fsim_step_host)
+    if (s->io_vel_pending) {
+      FSIM_CK(s, cudaStreamWaitEvent(s->stream, s->ev_io, 0));
+      s->io_vel_pending = false;
+    }
     FSIM_LAUNCH(s, "gather_particles", k_gather, nblk(n, 256), 256, 0, s->part[s->cur],
                 s->part[s->cur ^ 1], s->cap_p, s->vals[0], s->d_cnt);
     s->cur ^= 1;

@@ -124,6 +124,9 @@ _SIGS = {
     "fsim_pcg_solve": (C.c_int, [_P, C.POINTER(fsim_pcg_params), C.POINTER(fsim_pcg_stats)]),
     "fsim_step": (C.c_int, [_P, C.c_float, C.POINTER(fsim_pcg_params),
                             C.POINTER(fsim_step_stats)]),
+    "fsim_step_host": (C.c_int, [_P, C.c_float, C.POINTER(fsim_pcg_params), _P, _P, _P,
+                                 C.c_int64, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64),
+                                 C.POINTER(fsim_step_stats)]),
     "fsim_compute_dt": (C.c_int, [C.c_float, C.c_int32, C.c_float, C.POINTER(C.c_float),
                                   C.POINTER(C.c_float)]),
     "fsim_download_field": (C.c_int, [_P, C.c_int32, _P, _P]),
@@ -436,6 +439,26 @@ class Simulation:
         st = fsim_step_stats()
         self._ck(self.lib.fsim_step(self.h, C.c_float(dt), C.byref(params), C.byref(st)), "step")
         return st
+
+    def step_host(self, dt: float, params: fsim_pcg_params, pos, vel, gvel, out=None):
+        """fsim_step_host: upload (pos, vel, gvel), one step, download.  pos,
+        vel, gvel are (n, 3) float32 arrays (numpy, or any object exposing
+        data_ptr() and shape, e.g. pinned torch tensors); out = (pos, vel,
+        gvel) receives the result (default: new numpy arrays of n rows).
+        Returns (stats, particle count after the step)."""
+        def addr(a):
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+        n = int(pos.shape[0])
+        if out is None:
+            out = tuple(np.empty((n, 3), np.float32) for _ in range(3))
+        cap = int(out[0].shape[0])
+        st = fsim_step_stats()
+        got = C.c_int64()
+        self._ck(self.lib.fsim_step_host(self.h, C.c_float(dt), C.byref(params), addr(pos),
+                                         addr(vel), addr(gvel), n, addr(out[0]), addr(out[1]),
+                                         addr(out[2]), cap, C.byref(got), C.byref(st)),
+                 "step_host")
+        return st, got.value
 
     # -- downloads ----------------------------------------------------------
     def _dense_shape(self):

@@ -294,6 +294,21 @@ typedef struct fsim_step_stats {
  * run as fused device kernels.  stats may be NULL. */
 int fsim_step(fsim_t* sim, float dt, const fsim_pcg_params* params,
               fsim_step_stats* stats);
+/* One step on a host-resident particle state: the same results as
+ * fsim_upload_particles(pos, vel, gvel, n); fsim_step(dt, params, stats);
+ * fsim_download_particles(out_pos, out_vel, out_gvel, capacity, n_out) --
+ * the way the reference steps particles that live in its runtime's host
+ * variables (FlipDriver::RunOneStep, common/flip_app_sim.cc:211-254, with
+ * the particle store in host memory).  The copies overlap the step: the
+ * velocity upload runs while positions are binned and sorted, and the
+ * position download runs during the pressure solve (positions are final
+ * after the sort).  Outputs may alias the inputs of the same name.  Host
+ * buffers should be pinned for full copy bandwidth.  With sources or the
+ * tank boundary the three calls run in sequence. */
+int fsim_step_host(fsim_t* sim, float dt, const fsim_pcg_params* params, const float* pos,
+                   const float* vel, const float* gvel, int64_t n, float* out_pos,
+                   float* out_vel, float* out_gvel, int64_t capacity, int64_t* n_out,
+                   fsim_step_stats* stats);
 
 /* Global dt rule of FlipDriver::WhileAndComputeDt (flip_app_sim.cc:357-428)
  * for one partition: dt = min(cfl*inv_speed, 1/frame_step), raised to

@@ -272,3 +272,40 @@ def test_run_frames_equals_stepping_by_hand():
     assert a.time == pytest.approx(b.time)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("case", ["sorted", "shuffled", "in_place", "tank"])
+def test_step_host_equals_three_calls(case):
+    """fsim_step_host (copies overlapping the step) gives bit for bit what
+    upload + step + download give, for input already in cell order, input in
+    random order (rebinned while the velocity upload is still in flight),
+    outputs written over the inputs, and the tank boundary (sequential)."""
+    boundary = fsim.BOUNDARY_TANK if case == "tank" else fsim.BOUNDARY_BOX
+    orc = make_oracle(32, "dam_break", boundary=boundary, noise=2.0)
+    a = make_gpu(orc, boundary=boundary)
+    b = make_gpu(orc, boundary=boundary)
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 1500, tolerance=1e-5)
+    pos, vel, gvel = a.download_particles()
+    if case == "shuffled":
+        perm = np.random.default_rng(3).permutation(pos.shape[0])
+        pos, vel, gvel = pos[perm].copy(), vel[perm].copy(), gvel[perm].copy()
+    for _ in range(2):
+        dt = 0.004
+        a.upload_particles(pos, vel, gvel)
+        sa = a.step(dt, prm)
+        ra = a.download_particles()
+        if case == "in_place":
+            out = (pos.copy(), vel.copy(), gvel.copy())
+            sb, n = b.step_host(dt, prm, *out, out=out)
+        else:
+            out = tuple(np.full_like(pos, np.nan) for _ in range(3))
+            sb, n = b.step_host(dt, prm, pos, vel, gvel, out=out)
+        assert n == ra[0].shape[0] == sa.particles == sb.particles
+        assert sb.pcg.iterations == sa.pcg.iterations
+        for x, y in zip(ra, out):
+            assert np.array_equal(x, y[:n]), case
+        for x, y in zip(ra, b.download_particles()):
+            assert np.array_equal(x, y), case
+        pos, vel, gvel = (x.copy() for x in ra)
+    a.close()
+    b.close()
