@@ -56,7 +56,13 @@ ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
 # flushed before the launch) from one ncu capture of `bench.py --pcg-micro` on the 256^3
 # dam-break system (4.02 M unknowns); scaled by each step's unknowns.
-NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.85e6 / 4021250, "pcg_update": 61.16e6 / 4021250}
+NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 50.00e6 / 4021250, "pcg_update": 61.30e6 / 4021250}
+# The two launches of one PCG iteration (spmv then update) are reported as one unit: the
+# split of the iteration's work between them is a design choice (the update could take
+# x += alpha p or leave it), and their times are nearly equal.
+PCG_PAIRS = {"pcg_spmv": "pcg_update", "pcg_update": "pcg_spmv",
+             "pcg_spmv_mixed": "pcg_update_mixed", "pcg_update_mixed": "pcg_spmv_mixed",
+             "pcg_spmv_f64": "pcg_update_f64", "pcg_update_f64": "pcg_spmv_f64"}
 
 
 def peaks():
@@ -190,7 +196,7 @@ def run_gpu(args, rank, world):
         inv = st.next_inv_speed
     free_b, total_b = torch.cuda.mem_get_info(device)  # after warm-up: all buffers exist
     launches0 = sim.launch_count()
-    iters, rows = [], []
+    iters, rows, loop_ms = [], [], []
     barrier()
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -202,6 +208,7 @@ def run_gpu(args, rank, world):
             inv = st.next_inv_speed
             iters.append(st.pcg.iterations)
             rows.append(st.pcg.n_rows)
+            loop_ms.append(st.pcg.loop_ms)
         ev1.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -283,7 +290,8 @@ def run_gpu(args, rank, world):
     barrier()
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], device=f"cuda:{device}")
     sim.close()
-    return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, clocks=clk.summary(),
+    return dict(ms=ms, kt=kt, launches=launches, iters=iters, rows=rows, loop_ms=loop_ms,
+                clocks=clk.summary(),
                 device_memory_gb=(total_b - free_b) / 1e9,
                 piters=piters, prows=prows, prof_ms=prof_ms,
                 n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms, e2e_split=e2e_split,
@@ -291,28 +299,59 @@ def run_gpu(args, rank, world):
 
 
 def roofline(res):
+    """Roofline of the dominant kernel.
+
+    When the dominant kernel is one of the two PCG launches, the unit is one
+    PCG iteration (spmv + update): algorithmic bytes = both kernels' bytes per
+    unknown x unknowns, and the time is the iteration loops' device time in
+    the timed steps (CUDA events the library records on its stream around
+    each step's loop: fsim_pcg_stats.loop_ms).  The per-kernel split comes
+    from the profiled steps' per-launch events (host-launched, so slower than
+    the graph loop).  Otherwise the dominant kernel's profiled event time."""
     peak, src = peaks()
     kt = res["kt"]
     if not kt:
         return None
     top = max(kt.items(), key=lambda kv: kv[1][0])
     name, (tot_ms, nl) = top
-    total_iters = sum(res["piters"])
-    # bytes of each working launch = per-unknown bytes x that step's unknowns
-    out = {"bound": "hbm", "kernel": name, "peak": peak, "peak_source": src, "unit": "GB/s",
-           "share_of_step": tot_ms / res["prof_ms"] if res["prof_ms"] > 0 else None,
-           "traffic": None}
+    out = {"bound": "hbm", "peak": peak, "peak_source": src, "unit": "GB/s", "traffic": None}
+    if name in PCG_PAIRS and PCG_PAIRS[name] in kt and res.get("loop_ms") and sum(res["loop_ms"]) > 0:
+        names = sorted([name, PCG_PAIRS[name]], key=lambda k: "update" in k)  # spmv, update
+        per = sum(ALG_BYTES[k] for k in names)
+        its, rws, lms = res["iters"], res["rows"], res["loop_ms"]
+        tot_bytes = sum(per * r * it for r, it in zip(rws, its))
+        loop = sum(lms)
+        achieved = tot_bytes / (loop * 1e-3) / 1e9
+        n_rows = float(np.mean(rws))
+        out.update(kernel="pcg_iteration (" + " + ".join(names) + ", graph loop)",
+                   achieved=achieved, frac=achieved / peak, alg_bytes_per_unknown=per,
+                   alg_bytes_per_launch=per * n_rows, unknowns=n_rows,
+                   us_per_iteration=loop * 1e3 / max(sum(its), 1), working_launches=sum(its),
+                   share_of_step=loop / res["ms"] if res["ms"] > 0 else None,
+                   time_source="fsim_pcg_stats.loop_ms: CUDA events on the library stream, timed steps")
+        if all(k in NCU_TRAFFIC_PER_UNKNOWN for k in names):
+            out["traffic"] = sum(NCU_TRAFFIC_PER_UNKNOWN[k] for k in names) * n_rows
+            out["traffic_source"] = "ncu capture of the 256^3 system (spmv + update), scaled by unknowns"
+        pit = sum(res["piters"])
+        prow = sum(r * it for r, it in zip(res["prows"], res["piters"]))
+        out["per_kernel_profiled"] = {
+            k: {"us_per_launch": kt[k][0] * 1e3 / max(pit, 1),
+                "achieved": ALG_BYTES[k] * prow / (kt[k][0] * 1e-3) / 1e9}
+            for k in names}
+        return out
+    out.update(kernel=name, launches=nl,
+               share_of_step=tot_ms / res["prof_ms"] if res["prof_ms"] > 0 else None)
     if name in NCU_TRAFFIC_PER_UNKNOWN and res["prows"]:
         out["traffic"] = NCU_TRAFFIC_PER_UNKNOWN[name] * float(np.mean(res["prows"]))
         out["traffic_source"] = "ncu capture of the 256^3 system, scaled by unknowns"
     if name in ALG_BYTES and res["prows"]:
-        alg = ALG_BYTES[name] * float(np.mean(res["prows"]))  # per working launch
+        alg = ALG_BYTES[name] * float(np.mean(res["prows"]))
         tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["prows"], res["piters"]))
         achieved = tot_bytes / (tot_ms * 1e-3) / 1e9
-        out.update(achieved=achieved, frac=achieved / peak,
-                   alg_bytes_per_launch=alg, working_launches=total_iters, launches=nl)
+        out.update(achieved=achieved, frac=achieved / peak, alg_bytes_per_launch=alg,
+                   working_launches=sum(res["piters"]))
     else:
-        out.update(achieved=None, frac=None, launches=nl)
+        out.update(achieved=None, frac=None)
     return out
 
 

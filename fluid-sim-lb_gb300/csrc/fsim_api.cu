@@ -311,6 +311,8 @@ int fsim_destroy(fsim_t* s) {
     cudaStreamDestroy(s->io_stream);
   }
   if (s->ev_main) cudaEventDestroy(s->ev_main);
+  for (auto e : s->ev_loop)
+    if (e) cudaEventDestroy(e);
   if (s->ev_io) cudaEventDestroy(s->ev_io);
   dfree(s->io_stage);
   if (s->stream) cudaStreamDestroy(s->stream);

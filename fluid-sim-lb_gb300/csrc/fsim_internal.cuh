@@ -190,6 +190,9 @@ struct fsim_sim {
   // fsim_step_host: a second stream for the copies that overlap the step
   cudaStream_t io_stream = nullptr;
   cudaEvent_t ev_main = nullptr, ev_io = nullptr;
+  // around the PCG iteration loops (fsim_pcg_stats::loop_ms)
+  cudaEvent_t ev_loop[2] = {nullptr, nullptr};
+  double pcg_loop_ms = 0.0;
   float* io_stage = nullptr;   // AoS staging of the early position download
   int64_t io_stage_cap = 0;
   bool io_vel_pending = false; // vel upload in flight on io_stream (ev_io)

@@ -1736,6 +1736,30 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0) {
   return FSIM_OK;
 }
 
+// Device time of an iteration loop: events on the handle's stream around it,
+// read after the loop's own synchronisation; accumulated per solve.
+struct LoopTimer {
+  fsim_sim* s;
+  bool on = false;
+  explicit LoopTimer(fsim_sim* h) : s(h) {
+    if (!s->ev_loop[0]) {
+      if (cudaEventCreate(&s->ev_loop[0]) != cudaSuccess) s->ev_loop[0] = nullptr;
+      if (cudaEventCreate(&s->ev_loop[1]) != cudaSuccess) s->ev_loop[1] = nullptr;
+    }
+    on = s->ev_loop[0] && s->ev_loop[1] &&
+         cudaEventRecord(s->ev_loop[0], s->stream) == cudaSuccess;
+  }
+  void stop() {
+    if (on && cudaEventRecord(s->ev_loop[1], s->stream) == cudaSuccess) {
+      cudaEventSynchronize(s->ev_loop[1]);
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, s->ev_loop[0], s->ev_loop[1]) == cudaSuccess)
+        s->pcg_loop_ms += double(ms);
+    }
+    on = false;
+  }
+};
+
 // One inner solve: setup, then the iterations.  The iterations run as a CUDA
 // graph whose conditional WHILE node repeats {spmv, update}; the kernel head
 // that sets the stop flag clears the condition, so the whole loop runs
@@ -1772,10 +1796,12 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       ca.cond = 0;
       void* args[] = {&ca};
       ProfScope ps(s, nm_spmv);
+      LoopTimer lt(s);
       cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_pcg_loop<T, DM>),
                                                   dim3(unsigned(cgrid)), dim3(kHotThreads), args,
                                                   0, s->stream);
       if (e == cudaSuccess) {
+        lt.stop();
         s->launches += 1;
         FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                    s->stream));
@@ -1790,8 +1816,10 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   }
   const int it0 = setup ? 0 : s->h_sc->iter;  // iterations before this segment
   if (s->use_graphs && !s->profiling) {
+    LoopTimer lt(s);
     const int rc = run_graph_loop<T, DM>(s, a, wgrid, par0);
     if (rc == FSIM_OK) {
+      lt.stop();
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
@@ -1807,6 +1835,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   a.cond = 0;
   int chunk = 8;
   int64_t launched = par0;  // parity of the next iteration; tracks the device count
+  LoopTimer lt(s);
   for (;;) {
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                s->stream));
@@ -1824,6 +1853,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     }
     if (chunk < 64) chunk *= 2;
   }
+  lt.stop();
   return FSIM_OK;
 }
 
@@ -1848,6 +1878,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
     return fail(s, FSIM_ERR_INVALID, "bad pcg mode/precision");
   int rc = ensure_pcg_vectors(s, prm->precision);
   if (rc) return rc;
+  s->pcg_loop_ms = 0.0;
   const int grid = std::max(1, std::min(s->n_pleaf, s->max_blocks));
   PcgArgs a;
   memset(&a, 0, sizeof(a));
@@ -1965,6 +1996,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
     st->status = status;
     st->rr = final_rr;
     st->bb = bb;
+    st->loop_ms = s->pcg_loop_ms;
   }
   return FSIM_OK;
 }

@@ -54,7 +54,8 @@ class fsim_pcg_params(C.Structure):
 
 class fsim_pcg_stats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("refinements", C.c_int32), ("n_rows", C.c_int32),
-                ("status", C.c_int32), ("rr", C.c_double), ("bb", C.c_double)]
+                ("status", C.c_int32), ("rr", C.c_double), ("bb", C.c_double),
+                ("loop_ms", C.c_double)]
 
 
 class fsim_step_stats(C.Structure):

@@ -265,6 +265,9 @@ typedef struct fsim_pcg_stats {
   int32_t status;          /* FSIM_OK / NOT_CONVERGED / BREAKDOWN */
   double rr;               /* final r.r (fp64 residual in MIXED) */
   double bb;               /* b.b */
+  double loop_ms;          /* device time of the iteration loops (CUDA events on
+                              the handle's stream around them; setup and the
+                              MIXED replacement sweeps excluded) */
 } fsim_pcg_stats;
 /* Fills params with the reference defaults for the handle's domain:
  * ABSOLUTE, FP32, 1500 iterations, threshold N1*N2*N3*0.5e-8
