@@ -283,6 +283,8 @@ struct fsim_sim {
   // (measured slower than the graph loop at 256^3: 42.5 vs 38.9 us per
   // iteration; opt-in)
   bool use_coop = false;
+  // spmv with the own columns staged by bulk copies (FSIM_PCG_TMA=1)
+  bool use_tma = false;
   // register-pipelined hot kernels (next half leaf loaded during the
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;

@@ -1169,6 +1169,192 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   put_partials<DM, 1>(a, kPartPAp, v);
 }
 
+// ---- bulk-copy (TMA) staging of the own columns ---------------------------------
+// A half leaf's own r, p_{j-1} and flags are 1 KB + 1 KB + 256 B, contiguous.
+// Lane 0 of each warp copies them into a ring of kStages shared-memory stages
+// with cp.async.bulk (the copy engine of the SM, no registers and no
+// load/store-unit slots), kStages - 1 half leaves ahead; an mbarrier per stage
+// counts the bytes in.  The halo column and the z faces (scattered, 32 B and
+// 4 B per lane) are still loaded into registers one half leaf ahead.
+constexpr int kStages = 3;
+constexpr unsigned kMbarPolls = 1u << 22;  // bounded wait on a stage
+
+struct SpmvStage {
+  float r[256];
+  float p[256];
+  uint8_t f[256];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; false if the stage did not fill within kMbarPolls polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  for (unsigned i = 0; i < kMbarPolls; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+// Lane 0: copy half leaf hw's own columns into stage st.
+__device__ __forceinline__ void spmv_stage_issue(const PcgArgs& a, int hw, const float* r,
+                                                 const float* pold, SpmvStage& st,
+                                                 uint64_t* bar) {
+  const int64_t o = int64_t(hw >> 1) * 512 + (hw & 1) * 256;
+  mbar_expect_tx(bar, 2u * 1024u + 256u);
+  bulk_g2s(st.r, r + o, 1024u, bar);
+  bulk_g2s(st.p, pold + o, 1024u, bar);
+  bulk_g2s(st.f, a.flags + o, 256u, bar);
+}
+
+// k_pcg_spmv_pl with the own columns staged by bulk copies (fp32).
+template <int DM>
+__global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_constant__ PcgArgs a) {
+  using T = float;
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<2, PartT<DM>> hs;
+  __shared__ __align__(128) SpmvStage stage[kHotThreads / 32][kStages];
+  __shared__ __align__(8) uint64_t bars[kHotThreads / 32][kStages];
+  const int par = a.par;
+  const T* r = static_cast<const T*>(a.r);
+  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
+  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
+  const int qold = 1 + (par ^ 1), qnew = 1 + par;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  const int hw0 = blockIdx.x * wpb + w;
+  SpmvStage* stg = stage[w];
+  uint64_t* bar = bars[w];
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < kStages; ++q) mbar_init(&bar[q], 1u);
+    fence_async_smem();
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (int q = 0; q < kStages - 1; ++q) {
+      const int hq = hw0 + q * hstride;
+      if (hq < nhw) spmv_stage_issue(a, hq, r, pold, stg[q], &bar[q]);
+    }
+  }
+  head_issue<DM, 2>(hs, a, 0);
+  fill_diag_table<T>(tab);
+  SpmvIn<T> cur;  // halo and z faces only (rc, pc, f come from the stage)
+  int nbl = -1;
+  if (hw0 < nhw) {
+    int fs[6];
+    face_slots(face_slot_lane(a.nbr, hw0 >> 1, lane), fs);
+    nbl = hw0 + hstride < nhw ? face_slot_lane(a.nbr, (hw0 + hstride) >> 1, lane) : -1;
+    spmv_load_halo<T>(a, hw0, lane, fs, r, pold, qold, cur);
+  }
+  const HotHead head = spmv_head<DM>(hs, a);
+  bool ok = true;
+  if (head.done) {
+    // no work: drain the copies already issued before leaving
+    for (int q = 0; q < kStages - 1; ++q)
+      if (hw0 + q * hstride < nhw) mbar_wait(&bar[q], 0u);
+    return;
+  }
+  const T beta = T(head.s);
+  Tile<T>& tile = tiles[w];
+  Dot<DM> dp;
+  int k = 0;
+  for (int hw = hw0; hw < nhw; hw += hstride, ++k) {
+    // keep kStages - 1 half leaves in flight: refill the stage read last time
+    {
+      const int hq = hw + (kStages - 1) * hstride;
+      const int q = (k + kStages - 1) % kStages;
+      if (lane == 0 && hq < nhw) spmv_stage_issue(a, hq, r, pold, stg[q], &bar[q]);
+    }
+    const int hn = hw + hstride;
+    SpmvIn<T> nxt;
+    if (hn < nhw) {
+      int fs[6];
+      face_slots(nbl, fs);
+      spmv_load_halo<T>(a, hn, lane, fs, r, pold, qold, nxt);
+      nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
+    }
+    const int q = k % kStages;
+    if (!mbar_wait(&bar[q], unsigned((k / kStages) & 1))) ok = false;
+    const HalfLeaf h = half_pos(hw, lane);
+    {
+      const float4 a0 = reinterpret_cast<const float4*>(stg[q].r)[2 * lane];
+      const float4 a1 = reinterpret_cast<const float4*>(stg[q].r)[2 * lane + 1];
+      const float4 b0 = reinterpret_cast<const float4*>(stg[q].p)[2 * lane];
+      const float4 b1 = reinterpret_cast<const float4*>(stg[q].p)[2 * lane + 1];
+      cur.f = reinterpret_cast<const uint2*>(stg[q].f)[lane];
+      cur.rc.v[0] = a0.x; cur.rc.v[1] = a0.y; cur.rc.v[2] = a0.z; cur.rc.v[3] = a0.w;
+      cur.rc.v[4] = a1.x; cur.rc.v[5] = a1.y; cur.rc.v[6] = a1.z; cur.rc.v[7] = a1.w;
+      cur.pc.v[0] = b0.x; cur.pc.v[1] = b0.y; cur.pc.v[2] = b0.z; cur.pc.v[3] = b0.w;
+      cur.pc.v[4] = b1.x; cur.pc.v[5] = b1.y; cur.pc.v[6] = b1.z; cur.pc.v[7] = b1.w;
+    }
+    __syncwarp();
+    if (lane == 0) fence_async_smem();  // this stage's reads before its next bulk write
+    Col<T> P, H;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      P.v[z] = pnew_of<T>(tab, fbyte(cur.f, z), cur.rc.v[z], cur.pc.v[z], beta);
+      H.v[z] = pnew_of<T>(tab, fbyte(cur.hf, z), cur.hr.v[z], cur.hp.v[z], beta);
+    }
+    const T zm = pnew_of<T>(tab, cur.zf0, cur.zr0, cur.zq0, beta);
+    const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
+    const int64_t o = int64_t(h.s) * 512 + h.c;
+    stcol(pnew, o, P);
+    {
+      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
+      zw[0] = P.v[0];
+      zw[64] = P.v[7];
+    }
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, cur.f, zm, zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
+    cur.hf = nxt.hf;
+    cur.hr = nxt.hr;
+    cur.hp = nxt.hp;
+    cur.zf0 = nxt.zf0; cur.zf1 = nxt.zf1;
+    cur.zr0 = nxt.zr0; cur.zr1 = nxt.zr1;
+    cur.zq0 = nxt.zq0; cur.zq1 = nxt.zq1;
+  }
+  if (!ok && lane == 0) atomicExch(&a.sc->bar_err, 2u);  // a stage never filled
+  PartT<DM> v[1] = {dp.pvalue()};
+  put_partials<DM, 1>(a, kPartPAp, v);
+}
+
 template <typename T>
 struct UpdIn {
   uint2 f;
@@ -1676,6 +1862,36 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
     pres[o] = float(x[o]);
 }
 
+// The hot kernel pair of a solve: the bulk-copy staged spmv (FP32 dots,
+// FSIM_PCG_TMA=1), the register-pipelined pair (fp32 vectors), or the plain
+// pair (fp64 vectors, or FSIM_PCG_PIPE=0).
+template <typename T, int DM>
+void* spmv_kernel(const fsim_sim* s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if constexpr (DM == 0) {
+      if (s->use_pipe && s->use_tma) return reinterpret_cast<void*>(k_pcg_spmv_tma<DM>);
+    }
+    if (s->use_pipe) return reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM>);
+  }
+  return reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+}
+template <typename T, int DM>
+void* update_kernel(const fsim_sim* s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (s->use_pipe) return reinterpret_cast<void*>(k_pcg_update_pl<T, DM>);
+  }
+  return reinterpret_cast<void*>(k_pcg_update<T, DM>);
+}
+int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
+  fsim::ProfScope ps(s, name);
+  void* args[] = {&a};
+  const cudaError_t e = cudaLaunchKernel(fn, dim3(unsigned(grid)), dim3(kHotThreads), args, 0,
+                                         s->stream);
+  s->launches++;
+  if (e != cudaSuccess) return cuda_fail(s, e, name);
+  return FSIM_OK;
+}
+
 // Builds and launches graph = WHILE(cond){ (spmv; update) x kPassIters } on
 // the handle's stream: one pass runs kPassIters iterations of alternating
 // parity (their buffers are fixed by PcgArgs::par), and kernels launched
@@ -1684,7 +1900,7 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
 // FSIM_ERR_CUDA when the graph API refuses (the caller then polls from the
 // host).  Kernel launches inside the graph are counted by the caller from
 // the iteration count the solve reports.
-constexpr int kPassIters = 4;  // PCG iterations per pass of the graph's WHILE body
+constexpr int kPassIters = 8;  // PCG iterations per pass of the graph's WHILE body
 
 template <typename T, int DM>
 int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0) {
@@ -1714,12 +1930,7 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0) {
       kn.kernel.gridDim = dim3(unsigned(wgrid));
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
-      if ((s->use_pipe && sizeof(T) == 4))
-        kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update_pl<T, DM>)
-                                 : reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM>);
-      else
-        kn.kernel.func = (k & 1) ? reinterpret_cast<void*>(k_pcg_update<T, DM>)
-                                 : reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+      kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s) : spmv_kernel<T, DM>(s);
       cudaGraphNode_t n = nullptr;
       e = cudaGraphAddNode(&n, body, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &kn);
       prev = n;
@@ -1775,13 +1986,10 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   if (setup) FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
   const int wpb = kHotThreads / 32;
   int occ_a = 1, occ_b = 1;
-  if ((s->use_pipe && sizeof(T) == 4)) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_pcg_spmv_pl<T, DM>, kHotThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_pcg_update_pl<T, DM>, kHotThreads, 0);
-  } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_pcg_spmv<T, DM>, kHotThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_pcg_update<T, DM>, kHotThreads, 0);
-  }
+  void* const fn_spmv = spmv_kernel<T, DM>(s);
+  void* const fn_upd = update_kernel<T, DM>(s);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, fn_spmv, kHotThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, fn_upd, kHotThreads, 0);
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks, kMaxHotGrid}));
@@ -1828,6 +2036,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       // n / kPassIters + 1 passes ran
       const int64_t n = std::max(s->h_sc->iter - it0, 0);
       s->launches += 2 * kPassIters * (n / kPassIters + 1);
+      if (s->h_sc->bar_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG stage copy did not complete");
       return FSIM_OK;
     }
     s->use_graphs = false;  // fall back for the rest of this handle's life
@@ -1840,20 +2049,17 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                s->stream));
     FSIM_CK(s, cudaStreamSynchronize(s->stream));
-    if (s->h_sc->done) break;
+    if (s->h_sc->done || s->h_sc->bar_err) break;
     for (int c = 0; c < chunk; ++c, ++launched) {
       a.par = int(launched & 1);
-      if ((s->use_pipe && sizeof(T) == 4)) {
-        FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv_pl<T, DM>), wgrid, kHotThreads, 0, a);
-        FSIM_LAUNCH(s, nm_upd, (k_pcg_update_pl<T, DM>), wgrid, kHotThreads, 0, a);
-      } else {
-        FSIM_LAUNCH(s, nm_spmv, (k_pcg_spmv<T, DM>), wgrid, kHotThreads, 0, a);
-        FSIM_LAUNCH(s, nm_upd, (k_pcg_update<T, DM>), wgrid, kHotThreads, 0, a);
-      }
+      int rc = launch_hot(s, nm_spmv, fn_spmv, wgrid, a);
+      if (rc == FSIM_OK) rc = launch_hot(s, nm_upd, fn_upd, wgrid, a);
+      if (rc != FSIM_OK) return rc;
     }
     if (chunk < 64) chunk *= 2;
   }
   lt.stop();
+  if (s->h_sc->bar_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG stage copy did not complete");
   return FSIM_OK;
 }
 
