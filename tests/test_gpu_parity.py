@@ -309,3 +309,25 @@ def test_step_host_equals_three_calls(case):
         pos, vel, gvel = (x.copy() for x in ra)
     a.close()
     b.close()
+
+
+def test_step_host_capacity_and_empty():
+    """fsim_step_host with a too-small output reports FSIM_ERR_CAPACITY and
+    the particle count, leaving the state usable; an empty state steps."""
+    orc = make_oracle(16, "dam_break")
+    sim = make_gpu(orc)
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 1500, tolerance=1e-5)
+    pos, vel, gvel = sim.download_particles()
+    n = pos.shape[0]
+    small = tuple(np.empty((n // 2, 3), np.float32) for _ in range(3))
+    with pytest.raises(fsim.FsimError) as e:
+        sim.step_host(0.004, prm, pos, vel, gvel, out=small)
+    assert e.value.code == fsim.ERR_CAPACITY
+    m = sim.particle_count()
+    assert n // 2 < m <= n
+    p2, _, _ = sim.download_particles()
+    assert p2.shape == (m, 3)
+    z = np.zeros((0, 3), np.float32)
+    st, m = sim.step_host(0.004, prm, z, z, z, out=(z, z, z))
+    assert m == 0 and st.particles == 0
+    sim.close()
