@@ -317,6 +317,8 @@ int fsim_destroy(fsim_t* s) {
     if (e) cudaEventDestroy(e);
   if (s->ev_io) cudaEventDestroy(s->ev_io);
   dfree(s->io_stage);
+  if (s->p2g_nodes) cudaFree(s->p2g_nodes);
+  if (s->p2g_touch) cudaFree(s->p2g_touch);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return FSIM_OK;

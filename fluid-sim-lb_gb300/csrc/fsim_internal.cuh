@@ -187,6 +187,10 @@ struct fsim_sim {
   int dev = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  // P2G pass 1 output (k_grid.cu): per particle leaf the 10^3 node block
+  unsigned long long* p2g_nodes = nullptr;
+  uint32_t* p2g_touch = nullptr;
+  int64_t p2g_cap = 0;
   // fsim_step_host: a second stream for the copies that overlap the step
   cudaStream_t io_stream = nullptr;
   cudaEvent_t ev_main = nullptr, ev_io = nullptr;

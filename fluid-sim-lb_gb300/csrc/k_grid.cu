@@ -45,6 +45,8 @@ struct GridArgs {
   float* div;
   float dt, fx, fy, fz;
   int64_t* cnt;
+  unsigned long long* p2g_nodes;  // P2G pass 1 output: [particle leaf][6][1000]
+  uint32_t* p2g_touch;            // [particle leaf][32] touched bits of the 1000 nodes
 };
 
 __device__ __forceinline__ void origin_of(const GridArgs& a, int s, int o[3]) {
@@ -77,40 +79,51 @@ __device__ __forceinline__ float from_fix(unsigned long long v) {
   return float(double(static_cast<long long>(v)) * (1.0 / 4294967296.0));
 }
 
-template <bool FUSED>
-__global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a) {
-  __shared__ unsigned long long sv[3][512];
-  __shared__ unsigned long long sw[3][512];
-  __shared__ uint8_t touched[512];
-  __shared__ int nb[27];
-  const int s = blockIdx.x;
+// P2G in two passes, each particle visited once.
+//
+// Pass 1 (k_p2g_cells, one CTA per particle leaf): each thread takes whole
+// cells of the leaf.  Per component D the particles of a cell reach an
+// 18-node box (3 node positions on each tangential axis -- the stencil starts
+// at the cell or one below it, by the side of the cell centre the particle is
+// on -- and 2 on the normal axis); the thread sums the cell's particles into
+// that box in registers, in list order, and adds each reached node into the
+// CTA's 10^3 node block (the leaf's 8^3 nodes and the one-node layer around
+// them) with one fixed-point shared atomic.  The block is written out per
+// leaf: nodes[6][1000] (value sums for D = 0..2, then weight sums) and 1000
+// touched bits.
+//
+// Pass 2 (k_p2g_nodes, one CTA per grid leaf): each node adds its own leaf's
+// entry and the entries of the neighbour particle leaves whose outer layer
+// covers it (a face node 1, an edge node 3, a corner node 7), then
+// normalises.  Fixed-point sums are exact, so the result does not depend on
+// which pass or CTA added a term: it equals the one-pass sum over all cells.
+constexpr int kNodeBlock = 1000;  // 10^3 node positions, local coordinates -1..8
+
+__device__ __forceinline__ int node_index(int li, int lj, int lk) {
+  return ((li + 1) * 10 + (lj + 1)) * 10 + (lk + 1);
+}
+
+__global__ void __launch_bounds__(256) k_p2g_cells(const __grid_constant__ GridArgs a) {
+  __shared__ unsigned long long sv[3][kNodeBlock];
+  __shared__ unsigned long long sw[3][kNodeBlock];
+  __shared__ uint8_t touched[1024];
+  const int s = blockIdx.x;  // particle leaf
   const int tid = threadIdx.x;
-  int org[3];
-  origin_of(a, s, org);
-  if (tid < 27) nb[tid] = a.nbr[int64_t(s) * 27 + tid];
-  for (int v = tid; v < 512; v += 256) {
+  for (int v = tid; v < kNodeBlock; v += 256) {
     sv[0][v] = 0ull; sv[1][v] = 0ull; sv[2][v] = 0ull;
     sw[0][v] = 0ull; sw[1][v] = 0ull; sw[2][v] = 0ull;
-    touched[v] = 0;
   }
+  for (int v = tid; v < 1024; v += 256) touched[v] = 0;
   __syncthreads();
+  int org[3];
+  origin_of(a, s, org);
   const float* px = a.part;
   const int64_t cap = a.cap;
-  // Each thread takes whole cells.  Per component D the particles of a cell
-  // reach an 18-node box (3 node positions on each tangential axis -- the
-  // stencil starts at the cell or one below it, by the side of the cell
-  // centre the particle is on -- and 2 on the normal axis); the thread sums
-  // the cell's particles into that box in registers, in list order, and
-  // flushes each node with one fixed-point atomic.  Trilinear weights are the
-  // products of the per-axis linear weights.
-  for (int c = tid; c < 1000; c += 256) {
-    const int ci = c / 100 - 1, cj = (c / 10) % 10 - 1, ck = c % 10 - 1;  // local [-1,8]
-    const int ns = nb[nb_index(side(ci), side(cj), side(ck))];
-    if (ns < 0 || ns >= a.n_pleaf) continue;
-    const int g[3] = {org[0] + ci, org[1] + cj, org[2] + ck};
-    const int vox = ((g[0] & 7) << 6) | ((g[1] & 7) << 3) | (g[2] & 7);
-    const uint2 rg = a.cell_range[int64_t(ns) * 512 + vox];
+  for (int c = tid; c < 512; c += 256) {
+    const int cl[3] = {c >> 6, (c >> 3) & 7, c & 7};
+    const uint2 rg = a.cell_range[int64_t(s) * 512 + c];
     if (rg.x >= rg.y) continue;
+    const int g[3] = {org[0] + cl[0], org[1] + cl[1], org[2] + cl[2]};
 #pragma unroll
     for (int D = 0; D < 3; ++D) {
       // box extents: 3 on the tangential axes, 2 on the normal axis D
@@ -165,9 +178,9 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
           }
         }
       }
-      // flush the box nodes that lie in this leaf
-      const int b0 = g[0] - (D == 0 ? 0 : 1) - org[0], b1 = g[1] - (D == 1 ? 0 : 1) - org[1],
-                b2 = g[2] - (D == 2 ? 0 : 1) - org[2];
+      // flush the reached box nodes (local coordinates -1..8)
+      const int b0 = cl[0] - (D == 0 ? 0 : 1), b1 = cl[1] - (D == 1 ? 0 : 1),
+                b2 = cl[2] - (D == 2 ? 0 : 1);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         if (i >= e0) continue;
@@ -178,11 +191,8 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
           for (int k = 0; k < 3; ++k) {
             if (k >= e2) continue;
             const int t = (i * e1 + j) * e2 + k;
-            const int li = b0 + i, lj = b1 + j, lk = b2 + k;
-            if (!((reach >> t) & 1u) || (unsigned)li >= 8u || (unsigned)lj >= 8u ||
-                (unsigned)lk >= 8u)
-              continue;
-            const int o = (li << 6) | (lj << 3) | lk;
+            if (!((reach >> t) & 1u)) continue;
+            const int o = node_index(b0 + i, b1 + j, b2 + k);
             atomicAdd(&sv[D][o], to_fix(am[t]));
             atomicAdd(&sw[D][o], to_fix(aw[t]));
             touched[o] = 1;
@@ -192,20 +202,62 @@ __global__ void __launch_bounds__(256) k_p2g(const __grid_constant__ GridArgs a)
     }
   }
   __syncthreads();
+  unsigned long long* out = a.p2g_nodes + int64_t(s) * 6 * kNodeBlock;
+  for (int v = tid; v < kNodeBlock; v += 256) {
+#pragma unroll
+    for (int D = 0; D < 3; ++D) {
+      out[D * kNodeBlock + v] = sv[D][v];
+      out[(3 + D) * kNodeBlock + v] = sw[D][v];
+    }
+  }
+  for (int v = tid; v < 1024; v += 256) {
+    const unsigned bits = __ballot_sync(0xffffffffu, touched[v] != 0);
+    if ((tid & 31) == 0) a.p2g_touch[int64_t(s) * 32 + (v >> 5)] = bits;
+  }
+}
+
+template <bool FUSED>
+__global__ void __launch_bounds__(256) k_p2g_nodes(const __grid_constant__ GridArgs a) {
+  __shared__ int nb[27];
+  const int s = blockIdx.x;  // grid leaf
+  const int tid = threadIdx.x;
+  if (tid < 27) nb[tid] = a.nbr[int64_t(s) * 27 + tid];
+  __syncthreads();
+  int org[3];
+  origin_of(a, s, org);
   float* vel = a.vel + int64_t(s) * 1536;
   for (int v = tid; v < 512; v += 256) {
     const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
     const int g[3] = {org[0] + x, org[1] + y, org[2] + z};
-    const bool on = touched[v] != 0;
+    // this leaf's own block, then the neighbour particle leaves that cover
+    // the node with their outer layer
+    unsigned long long sv[3] = {0ull, 0ull, 0ull}, sw[3] = {0ull, 0ull, 0ull};
+    bool on = false;
+    const int dlo[3] = {x == 0 ? -1 : 0, y == 0 ? -1 : 0, z == 0 ? -1 : 0};
+    const int dhi[3] = {x == 7 ? 1 : 0, y == 7 ? 1 : 0, z == 7 ? 1 : 0};
+    for (int dx = dlo[0]; dx <= dhi[0]; ++dx)
+      for (int dy = dlo[1]; dy <= dhi[1]; ++dy)
+        for (int dz = dlo[2]; dz <= dhi[2]; ++dz) {
+          const int ns = nb[nb_index(dx, dy, dz)];
+          if (ns < 0 || ns >= a.n_pleaf) continue;
+          const int o = node_index(x - 8 * dx, y - 8 * dy, z - 8 * dz);
+          const unsigned long long* blk = a.p2g_nodes + int64_t(ns) * 6 * kNodeBlock;
+#pragma unroll
+          for (int D = 0; D < 3; ++D) {
+            sv[D] += blk[D * kNodeBlock + o];
+            sw[D] += blk[(3 + D) * kNodeBlock + o];
+          }
+          on |= (a.p2g_touch[int64_t(ns) * 32 + (o >> 5)] >> (o & 31)) & 1u;
+        }
     float val[3];
     float wsum[3];
 #pragma unroll
     for (int D = 0; D < 3; ++D) {
-      const float ws = from_fix(sw[D][v]);
+      const float ws = from_fix(sw[D]);
       wsum[D] = ws;
       // THRESH is a double literal in the reference: float ws < 1e-5 (double)
       // is ws <= 1e-5f
-      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(from_fix(sv[D][v]), ws)) : 0.f;
+      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(from_fix(sv[D]), ws)) : 0.f;
     }
     // marker: FLUID for in-box cells holding particles
     bool has = false;
@@ -582,18 +634,31 @@ GridArgs make_args(fsim_sim* s) {
   a.fy = s->cfg.force[1];
   a.fz = s->cfg.force[2];
   a.cnt = s->d_cnt;
+  a.p2g_nodes = s->p2g_nodes;
+  a.p2g_touch = s->p2g_touch;
   return a;
 }
 
 }  // namespace
 
 int launch_p2g(fsim_sim* s, bool fused, float dt) {
+  if (s->p2g_cap < s->cap_pleaf) {
+    if (s->p2g_nodes) cudaFree(s->p2g_nodes);
+    if (s->p2g_touch) cudaFree(s->p2g_touch);
+    s->p2g_nodes = nullptr;
+    s->p2g_touch = nullptr;
+    s->p2g_cap = 0;
+    FSIM_CK(s, cudaMalloc(&s->p2g_nodes, size_t(s->cap_pleaf) * 6 * kNodeBlock * 8));
+    FSIM_CK(s, cudaMalloc(&s->p2g_touch, size_t(s->cap_pleaf) * 32 * 4));
+    s->p2g_cap = s->cap_pleaf;
+  }
   GridArgs a = make_args(s);
   a.dt = dt;
+  FSIM_LAUNCH(s, fused ? "p2g_cells_fused" : "p2g_cells", k_p2g_cells, s->n_pleaf, 256, 0, a);
   if (fused)
-    FSIM_LAUNCH(s, "p2g_fused", k_p2g<true>, s->n_gleaf, 256, 0, a);
+    FSIM_LAUNCH(s, "p2g_fused", k_p2g_nodes<true>, s->n_gleaf, 256, 0, a);
   else
-    FSIM_LAUNCH(s, "p2g", k_p2g<false>, s->n_gleaf, 256, 0, a);
+    FSIM_LAUNCH(s, "p2g", k_p2g_nodes<false>, s->n_gleaf, 256, 0, a);
   return FSIM_OK;
 }
 
