@@ -75,8 +75,10 @@ constexpr float kFixScale = 4294967296.0f;  // 2^32
 __device__ __forceinline__ unsigned long long to_fix(float x) {
   return static_cast<unsigned long long>(__float2ll_rn(__fmul_rn(x, kFixScale)));
 }
+// The float nearest the fixed-point value (one rounding; the 2^-32 scaling is
+// exact for the sums a grid can hold).
 __device__ __forceinline__ float from_fix(unsigned long long v) {
-  return float(double(static_cast<long long>(v)) * (1.0 / 4294967296.0));
+  return __fmul_rn(__ll2float_rn(static_cast<long long>(v)), 1.0f / 4294967296.0f);
 }
 
 // P2G in two passes, each particle visited once.
