@@ -477,7 +477,7 @@ __device__ __forceinline__ int face_slot_lane(const int32_t* nbr, int s, int lan
   int q = 13;
   if (lane == 0) q = 4; else if (lane == 1) q = 22; else if (lane == 2) q = 10;
   else if (lane == 3) q = 16; else if (lane == 4) q = 12; else if (lane == 5) q = 14;
-  return (lane < 6) ? __ldg(nbr + int64_t(s) * 27 + q) : -1;
+  return (lane < 6) ? __ldg(nbr + (unsigned(s) * 27u + unsigned(q))) : -1;
 }
 __device__ __forceinline__ void face_slots(int mine, int out[6]) {
 #pragma unroll
@@ -1052,7 +1052,7 @@ template <typename T>
 __device__ __forceinline__ void spmv_load_own(const PcgArgs& a, int hw, int lane, const T* r,
                                               const T* pold, SpmvIn<T>& in) {
   const HalfLeaf h = half_pos(hw, lane);
-  const int64_t o = int64_t(h.s) * 512 + h.c;
+  const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
   in.f = ldflags(a.flags, o);
   ldcol(r, o, in.rc);
   ldcol(pold, o, in.pc);
@@ -1067,7 +1067,7 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
   const bool hv = hslot >= 0 && hslot < a.n_pleaf;
-  const int64_t hb = int64_t(hv ? hslot : 0) * 512 + hvox;
+  const unsigned hb = unsigned(hv ? hslot : 0) * 512u + unsigned(hvox);
   in.hf = make_uint2(0u, 0u);
   if (hv) {
     in.hf = ldflags(a.flags, hb);
@@ -1080,10 +1080,10 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   const int zs0 = fs[4], zs1 = fs[5];
   const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
   const T* zf = static_cast<const T*>(a.zf);
-  const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + h.fidx;
-  const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + h.fidx;
-  in.zf0 = zv0 ? ldv(a.zff + int64_t(zs0) * 128 + 64 + h.fidx) : uint8_t(0);
-  in.zf1 = zv1 ? ldv(a.zff + int64_t(zs1) * 128 + h.fidx) : uint8_t(0);
+  const unsigned zo0 = unsigned(zv0 ? zs0 : 0) * 384u + 64u + unsigned(h.fidx);
+  const unsigned zo1 = unsigned(zv1 ? zs1 : 0) * 384u + unsigned(h.fidx);
+  in.zf0 = zv0 ? ldv(a.zff + (unsigned(zs0) * 128u + 64u + unsigned(h.fidx))) : uint8_t(0);
+  in.zf1 = zv1 ? ldv(a.zff + (unsigned(zs1) * 128u + unsigned(h.fidx))) : uint8_t(0);
   in.zr0 = zv0 ? ldv(zf + zo0) : T(0);
   in.zr1 = zv1 ? ldv(zf + zo1) : T(0);
   in.zq0 = zv0 ? ldv(zf + zo0 + 128 * qold) : T(0);
@@ -1147,10 +1147,10 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
     }
     const T zm = pnew_of<T>(tab, cur.zf0, cur.zr0, cur.zq0, beta);
     const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
-    const int64_t o = int64_t(h.s) * 512 + h.c;
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(pnew, o, P);
     {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
+      T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
       zw[0] = P.v[0];
       zw[64] = P.v[7];
     }
@@ -1328,10 +1328,10 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_co
     }
     const T zm = pnew_of<T>(tab, cur.zf0, cur.zr0, cur.zq0, beta);
     const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
-    const int64_t o = int64_t(h.s) * 512 + h.c;
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(pnew, o, P);
     {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
+      T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
       zw[0] = P.v[0];
       zw[64] = P.v[7];
     }
@@ -1366,7 +1366,7 @@ template <typename T>
 __device__ __forceinline__ void upd_load_own(const PcgArgs& a, int hw, int lane, const T* p,
                                              const T* x, const T* r, UpdIn<T>& in) {
   const HalfLeaf h = half_pos(hw, lane);
-  const int64_t o = int64_t(h.s) * 512 + h.c;
+  const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
   in.f = ldflags(a.flags, o);
   ldcol(p, o, in.P);
   ldcol(x, o, in.x);
@@ -1380,15 +1380,15 @@ __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
   if (hslot >= 0 && hslot < a.n_pleaf) {
-    ldcol(p, int64_t(hslot) * 512 + hvox, in.H);
+    ldcol(p, unsigned(hslot) * 512u + unsigned(hvox), in.H);
   } else {
 #pragma unroll
     for (int z = 0; z < 8; ++z) in.H.v[z] = T(0);
   }
   const int zs0 = fs[4], zs1 = fs[5];
-  const T* zfp = static_cast<const T*>(a.zf) + 128 * qcur + h.fidx;
-  in.zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? ldv(zfp + int64_t(zs0) * 384 + 64) : T(0);
-  in.zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + int64_t(zs1) * 384) : T(0);
+  const T* zfp = static_cast<const T*>(a.zf) + (128u * unsigned(qcur) + unsigned(h.fidx));
+  in.zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? ldv(zfp + (unsigned(zs0) * 384u + 64u)) : T(0);
+  in.zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + unsigned(zs1) * 384u) : T(0);
 }
 
 template <typename T>
@@ -1456,11 +1456,11 @@ __global__ void __launch_bounds__(kHotThreads, 4)
       drr.add(cur.r.v[z], cur.r.v[z]);
       drz.add(cur.r.v[z], tmul(tab[g & 15].inv, cur.r.v[z]));
     }
-    const int64_t o = int64_t(h.s) * 512 + h.c;
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(x, o, cur.x);
     stcol(r, o, cur.r);
     {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + h.fidx;
+      T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + unsigned(h.fidx));
       zw[0] = cur.r.v[0];
       zw[64] = cur.r.v[7];
     }
