@@ -245,6 +245,9 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   s->max_blocks = std::max(1, s->num_sms) * 16;  // a multiple of 4: partial rows stay 16-byte aligned
   // FSIM_PCG_GRAPH=0 turns the graph loop off (host polling)
   if (const char* g = std::getenv("FSIM_PCG_GRAPH")) s->use_graphs = g[0] != '0';
+  // FSIM_PCG_PDL=0: plain edges between the graph's kernel nodes (default:
+  // programmatic edges, each kernel launching while its predecessor finishes)
+  if (const char* c = std::getenv("FSIM_PCG_PDL")) s->use_pdl = c[0] != '0';
   // FSIM_PCG_COOP=1: the PCG iterations as one persistent cooperative kernel
   if (const char* c = std::getenv("FSIM_PCG_COOP")) s->use_coop = c[0] == '1';
   // FSIM_PCG_TMA=1: the spmv with bulk-copy staged own columns (FP32 dots)

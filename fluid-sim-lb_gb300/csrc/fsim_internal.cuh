@@ -283,6 +283,8 @@ struct fsim_sim {
 
   // PCG iterations as a CUDA graph with a conditional WHILE node
   bool use_graphs = true;
+  // its kernel nodes joined by programmatic (early-launch) edges
+  bool use_pdl = true;
   // PCG iterations as one cooperative persistent kernel with grid barriers
   // (measured slower than the graph loop at 256^3: 42.5 vs 38.9 us per
   // iteration; opt-in)

@@ -623,6 +623,19 @@ __device__ __forceinline__ T pnew_of(const DiagInv<T>* tab, uint8_t f, T r, T po
   return tadd(tmul(tab[f & 15].inv, r), tmul(beta, po));
 }
 
+// Programmatic dependent launch (the graph's edges are of programmatic type
+// unless FSIM_PCG_PDL=0): a hot kernel may start while its predecessor's last CTAs
+// finish.  Before pdl_wait() it reads only data written two or more launches
+// back (flags, the neighbour table, and the one vector its predecessor does
+// not write); pdl_wait() returns once the predecessor grid has completed and
+// its writes are visible (at once without a programmatic edge).  Each kernel
+// lets its successor launch only after its own wait, so a kernel never runs
+// beside the one two launches back.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 // ---- deferred reductions ------------------------------------------------------
 // The hot kernels do not finish their own dot products.  Each CTA writes its
 // block partial and exits; every CTA of the NEXT kernel sums all of them in
@@ -841,6 +854,8 @@ __device__ __forceinline__ void put_partials(const PcgArgs& a, int row0, PartT<D
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_spmv(const __grid_constant__ PcgArgs a) {
+  pdl_wait();  // reads its predecessor's outputs from the start
+  pdl_trigger();
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
   __shared__ HeadStage<2, PartT<DM>> hs;
@@ -946,6 +961,8 @@ __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
 template <typename T, int DM>
 __global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
     k_pcg_update(const __grid_constant__ PcgArgs a) {
+  pdl_wait();  // reads its predecessor's outputs from the start
+  pdl_trigger();
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
   __shared__ HeadStage<1, PartT<DM>> hs;
@@ -1111,17 +1128,27 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  head_issue<DM, 2>(hs, a, 0);
   fill_diag_table<T>(tab);
   SpmvIn<T> cur;
   int nbl = -1;
+  int fs[6];
+  // before the wait: the neighbour table, flags and p_{j-1} (written by the
+  // spmv two launches back) of the first half leaf
   if (hw < nhw) {
-    // own column first: its loads fly while the face slots arrive
     const int nb0 = face_slot_lane(a.nbr, hw >> 1, lane);
-    spmv_load_own<T>(a, hw, lane, r, pold, cur);
+    const HalfLeaf h = half_pos(hw, lane);
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
+    cur.f = ldflags(a.flags, o);
+    ldcol(pold, o, cur.pc);
     nbl = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
-    int fs[6];
     face_slots(nb0, fs);
+  }
+  pdl_wait();
+  pdl_trigger();
+  head_issue<DM, 2>(hs, a, 0);
+  if (hw < nhw) {
+    const HalfLeaf h = half_pos(hw, lane);
+    ldcol(r, unsigned(h.s) * 512u + unsigned(h.c), cur.rc);
     spmv_load_halo<T>(a, hw, lane, fs, r, pold, qold, cur);
   }
   const HotHead head = spmv_head<DM>(hs, a);
@@ -1238,6 +1265,8 @@ __device__ __forceinline__ void spmv_stage_issue(const PcgArgs& a, int hw, const
 // k_pcg_spmv_pl with the own columns staged by bulk copies (fp32).
 template <int DM>
 __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_constant__ PcgArgs a) {
+  pdl_wait();  // reads its predecessor's outputs from the start
+  pdl_trigger();
   using T = float;
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
@@ -1414,16 +1443,28 @@ __global__ void __launch_bounds__(kHotThreads, 4)
   const int wpb = kHotThreads / 32;
   const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
   int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
-  head_issue<DM, 1>(hs, a, kPartPAp);
   fill_diag_table<T>(tab);
   UpdIn<T> cur;
   int nbl = -1;
+  int fs[6];
+  // before the wait: the neighbour table, flags, x and r (written by the
+  // update two launches back) of the first half leaf
   if (hw < nhw) {
     const int nb0 = face_slot_lane(a.nbr, hw >> 1, lane);
-    upd_load_own<T>(a, hw, lane, p, x, r, cur);
+    const HalfLeaf h = half_pos(hw, lane);
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
+    cur.f = ldflags(a.flags, o);
+    ldcol(x, o, cur.x);
+    ldcol(r, o, cur.r);
     nbl = hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
-    int fs[6];
     face_slots(nb0, fs);
+  }
+  pdl_wait();
+  pdl_trigger();
+  head_issue<DM, 1>(hs, a, kPartPAp);
+  if (hw < nhw) {
+    const HalfLeaf h = half_pos(hw, lane);
+    ldcol(p, unsigned(h.s) * 512u + unsigned(h.c), cur.P);
     upd_load_halo<T>(a, hw, lane, fs, p, qcur, cur);
   }
   const HotHead head = update_head<DM>(hs, a);
@@ -1903,7 +1944,7 @@ int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
 constexpr int kPassIters = 8;  // PCG iterations per pass of the graph's WHILE body
 
 template <typename T, int DM>
-int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0) {
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -1931,8 +1972,14 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0) {
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
       kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s) : spmv_kernel<T, DM>(s);
+      cudaGraphEdgeData ed = {};
+      if (pdl) {  // the successor may launch while this kernel's last CTAs finish
+        ed.from_port = cudaGraphKernelNodePortProgrammatic;
+        ed.type = cudaGraphDependencyTypeProgrammatic;
+      }
       cudaGraphNode_t n = nullptr;
-      e = cudaGraphAddNode(&n, body, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &kn);
+      e = cudaGraphAddNode(&n, body, prev ? &prev : nullptr, prev ? &ed : nullptr, prev ? 1 : 0,
+                           &kn);
       prev = n;
     }
   }
@@ -2025,7 +2072,12 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   const int it0 = setup ? 0 : s->h_sc->iter;  // iterations before this segment
   if (s->use_graphs && !s->profiling) {
     LoopTimer lt(s);
-    const int rc = run_graph_loop<T, DM>(s, a, wgrid, par0);
+    int rc = FSIM_ERR_CUDA;
+    if (s->use_pdl) {
+      rc = run_graph_loop<T, DM>(s, a, wgrid, par0, true);
+      if (rc != FSIM_OK) s->use_pdl = false;  // programmatic edges refused: plain edges
+    }
+    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, par0, false);
     if (rc == FSIM_OK) {
       lt.stop();
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
