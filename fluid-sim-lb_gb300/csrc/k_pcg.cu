@@ -1145,12 +1145,12 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   }
   pdl_wait();
   pdl_trigger();
-  head_issue<DM, 2>(hs, a, 0);
   if (hw < nhw) {
     const HalfLeaf h = half_pos(hw, lane);
     ldcol(r, unsigned(h.s) * 512u + unsigned(h.c), cur.rc);
     spmv_load_halo<T>(a, hw, lane, fs, r, pold, qold, cur);
   }
+  head_issue<DM, 2>(hs, a, 0);
   const HotHead head = spmv_head<DM>(hs, a);
   if (head.done) return;
   const T beta = T(head.s);
@@ -1461,12 +1461,12 @@ __global__ void __launch_bounds__(kHotThreads, 4)
   }
   pdl_wait();
   pdl_trigger();
-  head_issue<DM, 1>(hs, a, kPartPAp);
   if (hw < nhw) {
     const HalfLeaf h = half_pos(hw, lane);
     ldcol(p, unsigned(h.s) * 512u + unsigned(h.c), cur.P);
     upd_load_halo<T>(a, hw, lane, fs, p, qcur, cur);
   }
+  head_issue<DM, 1>(hs, a, kPartPAp);
   const HotHead head = update_head<DM>(hs, a);
   if (head.done) return;
   const T alpha = T(head.s);
