@@ -516,7 +516,10 @@ def pcg_micro(args):
         sim.synchronize()
         kt = sim.kernel_times()
         sim.set_profiling(False)
-        out[name + "_us_per_launch"] = {n: round(v[0] / max(v[1], 1) * 1e3, 2)
+        # per iteration: the host launches chunks of iterations, and launches
+        # after the stop flag return at once, so the time is divided by the
+        # k working launches rather than by all launches
+        out[name + "_us_per_launch"] = {n: round(v[0] / k * 1e3, 2)
                                         for n, v in kt.items() if v[1] >= k // 2}
     for prec, name in ((fsim.PREC_FP32, "fp32"), (fsim.PREC_MIXED, "mixed")):
         sim.synchronize()
