@@ -705,12 +705,17 @@ int upload_overlapped(fsim_sim* s, const float* pos, const float* vel, const flo
   if ((rc = ensure_particle_capacity(s, n))) return rc;
   float* stage = s->part[s->cur ^ 1];
   if (n > 0) {
-    FSIM_CK(s, cudaEventRecord(s->ev_main, s->stream));
-    FSIM_CK(s, cudaStreamWaitEvent(s->io_stream, s->ev_main, 0));
     for (int f = 0; f < 3; f += 2) {  // pos, gvel
       const float* src = f == 0 ? pos : gvel;
       FSIM_CK(s, cudaMemcpyAsync(stage + size_t(f) * 3 * s->cap_p, src, size_t(n) * 12,
                                  cudaMemcpyHostToDevice, s->stream));
+      // the velocity copy starts when the gvel copy is done: run at the same
+      // time, the three copies would share the host link and delay the two
+      // the rebinning and the advection need first
+      if (f == 2) {
+        FSIM_CK(s, cudaEventRecord(s->ev_main, s->stream));
+        FSIM_CK(s, cudaStreamWaitEvent(s->io_stream, s->ev_main, 0));
+      }
       FSIM_LAUNCH(s, "aos_to_soa", k_aos_to_soa, unsigned((n + 255) / 256), 256, 0,
                   stage + size_t(f) * 3 * s->cap_p, s->part[s->cur], n, s->cap_p, 3 * f);
     }
