@@ -170,6 +170,8 @@ def run_gpu(args, rank, world):
 
     device = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(device)
+    if args.lib:
+        fsim._lib = fsim.load_library(args.lib)  # a variant build of the library
     wl = WORKLOADS[args.workload]
     sim = make_sim(wl, args, device)
     n_particles = sim.particle_count()
@@ -622,7 +624,7 @@ def main():
     ap.add_argument("--pcg-micro", action="store_true",
                     help="per-kernel PCG times on one step's system (fixed iteration count)")
     ap.add_argument("--micro-iters", type=int, default=300)
-    ap.add_argument("--lib", default=None, help="--pcg-micro: path of a variant libfsim.so")
+    ap.add_argument("--lib", default=None, help="path of a variant libfsim.so (A/B runs)")
     ap.add_argument("--adjoint-check", action="store_true",
                     help="differentiable rollout: adjoint vs central differences")
     ap.add_argument("--adjoint-n", type=int, default=128)
