@@ -2073,7 +2073,12 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   if (s->use_graphs && !s->profiling) {
     LoopTimer lt(s);
     int rc = FSIM_ERR_CUDA;
-    if (s->use_pdl) {
+    // Programmatic edges pay off only for the pipelined fp32-vector kernels,
+    // which prefetch before their wait; the others wait at their first
+    // instruction, and their early-launched CTAs only hold SM slots (the
+    // FP64 solve measured 20% slower with them).
+    const bool pdl = s->use_pdl && std::is_same<T, float>::value && s->use_pipe && !s->use_tma;
+    if (pdl) {
       rc = run_graph_loop<T, DM>(s, a, wgrid, par0, true);
       if (rc != FSIM_OK) s->use_pdl = false;  // programmatic edges refused: plain edges
     }
