@@ -252,6 +252,8 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if (const char* c = std::getenv("FSIM_PCG_COOP")) s->use_coop = c[0] == '1';
   // FSIM_PCG_TMA=1: the spmv with bulk-copy staged own columns (FP32 dots)
   if (const char* c = std::getenv("FSIM_PCG_TMA")) s->use_tma = c[0] == '1';
+  // FSIM_PCG_ZDIRECT=0/1: z-face planes or direct reads (default: by system size)
+  if (const char* c = std::getenv("FSIM_PCG_ZDIRECT")) s->zdirect = c[0] == '1' ? 1 : 0;
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels
   if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
   for (int a = 0; a < 3; ++a) {

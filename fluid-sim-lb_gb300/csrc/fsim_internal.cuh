@@ -291,6 +291,9 @@ struct fsim_sim {
   bool use_coop = false;
   // spmv with the own columns staged by bulk copies (FSIM_PCG_TMA=1)
   bool use_tma = false;
+  // z-face neighbours of the pipelined kernels: -1 by system size, 0 planes,
+  // 1 direct reads (FSIM_PCG_ZDIRECT)
+  int zdirect = -1;
   // register-pipelined hot kernels (next half leaf loaded during the
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;

@@ -298,6 +298,7 @@ struct PcgArgs {
   float* partf;     // fp32 / double-float block partials of the hot kernels (FP32, MIXED)
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
   int par;          // spmv / update: parity of the iteration this launch serves
+  int zdirect;      // pipelined kernels: z-face neighbours read from the vectors, no planes
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
 };
 
@@ -654,6 +655,7 @@ __device__ __forceinline__ void pdl_trigger() {
 // trip of the head hides under the first loads from HBM.
 constexpr int kPartPAp = 3;       // part[] row of the spmv's p.Ap partials
 constexpr int kMaxHotGrid = 1022; // hot grids stay below this (even) size
+constexpr int kZDirectLeaves = 16384;  // above this many particle leaves: direct z-face reads
 
 struct HotHead {
   int done;
@@ -1096,6 +1098,19 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   }
   const int zs0 = fs[4], zs1 = fs[5];
   const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+  if (a.zdirect) {
+    // the -z neighbour's cell (x, y, 7) and the +z neighbour's (x, y, 0): their
+    // leaves are processed at about the same time, so the loads hit L2
+    const unsigned c0 = unsigned(zv0 ? zs0 : 0) * 512u + unsigned(h.c) + 7u;
+    const unsigned c1 = unsigned(zv1 ? zs1 : 0) * 512u + unsigned(h.c);
+    in.zf0 = zv0 ? ldv(a.flags + c0) : uint8_t(0);
+    in.zf1 = zv1 ? ldv(a.flags + c1) : uint8_t(0);
+    in.zr0 = zv0 ? ldv(r + c0) : T(0);
+    in.zr1 = zv1 ? ldv(r + c1) : T(0);
+    in.zq0 = zv0 ? ldv(pold + c0) : T(0);
+    in.zq1 = zv1 ? ldv(pold + c1) : T(0);
+    return;
+  }
   const T* zf = static_cast<const T*>(a.zf);
   const unsigned zo0 = unsigned(zv0 ? zs0 : 0) * 384u + 64u + unsigned(h.fidx);
   const unsigned zo1 = unsigned(zv1 ? zs1 : 0) * 384u + unsigned(h.fidx);
@@ -1176,7 +1191,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
     const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
     const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(pnew, o, P);
-    {
+    if (!a.zdirect) {  // publish the z faces for the neighbours
       T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
       zw[0] = P.v[0];
       zw[64] = P.v[7];
@@ -1359,7 +1374,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_co
     const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
     const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(pnew, o, P);
-    {
+    if (!a.zdirect) {  // publish the z faces for the neighbours
       T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
       zw[0] = P.v[0];
       zw[64] = P.v[7];
@@ -1415,9 +1430,15 @@ __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane
     for (int z = 0; z < 8; ++z) in.H.v[z] = T(0);
   }
   const int zs0 = fs[4], zs1 = fs[5];
+  const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+  if (a.zdirect) {
+    in.zm = zv0 ? ldv(p + (unsigned(zs0) * 512u + unsigned(h.c) + 7u)) : T(0);
+    in.zp = zv1 ? ldv(p + (unsigned(zs1) * 512u + unsigned(h.c))) : T(0);
+    return;
+  }
   const T* zfp = static_cast<const T*>(a.zf) + (128u * unsigned(qcur) + unsigned(h.fidx));
-  in.zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? ldv(zfp + (unsigned(zs0) * 384u + 64u)) : T(0);
-  in.zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? ldv(zfp + unsigned(zs1) * 384u) : T(0);
+  in.zm = zv0 ? ldv(zfp + (unsigned(zs0) * 384u + 64u)) : T(0);
+  in.zp = zv1 ? ldv(zfp + unsigned(zs1) * 384u) : T(0);
 }
 
 template <typename T>
@@ -1500,7 +1521,7 @@ __global__ void __launch_bounds__(kHotThreads, 4)
     const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(x, o, cur.x);
     stcol(r, o, cur.r);
-    {
+    if (!a.zdirect) {
       T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + unsigned(h.fidx));
       zw[0] = cur.r.v[0];
       zw[64] = cur.r.v[7];
@@ -2038,6 +2059,12 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, fn_spmv, kHotThreads, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, fn_upd, kHotThreads, 0);
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
+  // Large systems: the pipelined kernels read z-face neighbours from the
+  // vectors (L2 hits) instead of the published planes, which no longer fit
+  // in L2 and cost about 4 B of DRAM traffic per unknown and iteration.
+  a.zdirect = (std::is_same<T, float>::value && s->use_pipe &&
+               (s->zdirect > 0 || (s->zdirect < 0 && a.n_pleaf > kZDirectLeaves)))
+                  ? 1 : 0;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks, kMaxHotGrid}));
   if (s->use_coop && !s->profiling) {

@@ -104,7 +104,7 @@ def test_loop_variants_agree(monkeypatch):
     persistent loop sums its partials over its own grid (equal to 1e-5)."""
     variants = (("graph", {}), ("host", {"FSIM_PCG_GRAPH": "0"}),
                 ("unpiped", {"FSIM_PCG_PIPE": "0"}), ("tma", {"FSIM_PCG_TMA": "1"}),
-                ("plain_edges", {"FSIM_PCG_PDL": "0"}),
+                ("plain_edges", {"FSIM_PCG_PDL": "0"}), ("zdirect", {"FSIM_PCG_ZDIRECT": "1"}),
                 ("coop", {"FSIM_PCG_COOP": "1"}))
     solves = ((fsim.PREC_FP32, 1e-5), (fsim.PREC_MIXED, 1e-7), (fsim.PREC_FP64, 1e-7))
     got = {}
@@ -121,7 +121,7 @@ def test_loop_variants_agree(monkeypatch):
             sim.close()
     for prec, _ in solves:
         it, rr, x = got["graph", prec]
-        for name in ("host", "unpiped", "tma", "plain_edges"):
+        for name in ("host", "unpiped", "tma", "plain_edges", "zdirect"):
             it2, rr2, x2 = got[name, prec]
             assert it2 == it and rr2 == rr and np.array_equal(x2, x), (name, prec)
         it2, rr2, x2 = got["coop", prec]
