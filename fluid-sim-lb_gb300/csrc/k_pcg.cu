@@ -298,7 +298,6 @@ struct PcgArgs {
   float* partf;     // fp32 / double-float block partials of the hot kernels (FP32, MIXED)
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
   int par;          // spmv / update: parity of the iteration this launch serves
-  int zdirect;      // pipelined kernels: z-face neighbours read from the vectors, no planes
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
 };
 
@@ -1078,7 +1077,9 @@ __device__ __forceinline__ void spmv_load_own(const PcgArgs& a, int hw, int lane
 }
 
 // ... and the halo column and z faces, addressed through the face slots.
-template <typename T>
+// ZD: z-face neighbours read from the vectors (large systems) instead of the
+// published planes.
+template <typename T, bool ZD>
 __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lane, const int fs[6],
                                                const T* r, const T* pold, int qold,
                                                SpmvIn<T>& in) {
@@ -1098,7 +1099,7 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   }
   const int zs0 = fs[4], zs1 = fs[5];
   const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
-  if (a.zdirect) {
+  if constexpr (ZD) {
     // the -z neighbour's cell (x, y, 7) and the +z neighbour's (x, y, 0): their
     // leaves are processed at about the same time, so the loads hit L2
     const unsigned c0 = unsigned(zv0 ? zs0 : 0) * 512u + unsigned(h.c) + 7u;
@@ -1122,14 +1123,14 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   in.zq1 = zv1 ? ldv(zf + zo1 + 128 * qold) : T(0);
 }
 
-template <typename T>
+template <typename T, bool ZD>
 __device__ __forceinline__ void spmv_load(const PcgArgs& a, int hw, int lane, const int fs[6],
                                           const T* r, const T* pold, int qold, SpmvIn<T>& in) {
   spmv_load_own<T>(a, hw, lane, r, pold, in);
-  spmv_load_halo<T>(a, hw, lane, fs, r, pold, qold, in);
+  spmv_load_halo<T, ZD>(a, hw, lane, fs, r, pold, qold, in);
 }
 
-template <typename T, int DM>
+template <typename T, int DM, bool ZD>
 __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
   __shared__ DiagInv<T> tab[16];
@@ -1163,7 +1164,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   if (hw < nhw) {
     const HalfLeaf h = half_pos(hw, lane);
     ldcol(r, unsigned(h.s) * 512u + unsigned(h.c), cur.rc);
-    spmv_load_halo<T>(a, hw, lane, fs, r, pold, qold, cur);
+    spmv_load_halo<T, ZD>(a, hw, lane, fs, r, pold, qold, cur);
   }
   head_issue<DM, 2>(hs, a, 0);
   const HotHead head = spmv_head<DM>(hs, a);
@@ -1177,7 +1178,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
     if (hn < nhw) {
       int fs[6];
       face_slots(nbl, fs);
-      spmv_load<T>(a, hn, lane, fs, r, pold, qold, nxt);
+      spmv_load<T, ZD>(a, hn, lane, fs, r, pold, qold, nxt);
       nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
     }
     const HalfLeaf h = half_pos(hw, lane);
@@ -1191,7 +1192,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
     const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
     const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(pnew, o, P);
-    if (!a.zdirect) {  // publish the z faces for the neighbours
+    if constexpr (!ZD) {  // publish the z faces for the neighbours
       T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
       zw[0] = P.v[0];
       zw[64] = P.v[7];
@@ -1319,7 +1320,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_co
     int fs[6];
     face_slots(face_slot_lane(a.nbr, hw0 >> 1, lane), fs);
     nbl = hw0 + hstride < nhw ? face_slot_lane(a.nbr, (hw0 + hstride) >> 1, lane) : -1;
-    spmv_load_halo<T>(a, hw0, lane, fs, r, pold, qold, cur);
+    spmv_load_halo<T, false>(a, hw0, lane, fs, r, pold, qold, cur);
   }
   const HotHead head = spmv_head<DM>(hs, a);
   bool ok = true;
@@ -1345,7 +1346,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_co
     if (hn < nhw) {
       int fs[6];
       face_slots(nbl, fs);
-      spmv_load_halo<T>(a, hn, lane, fs, r, pold, qold, nxt);
+      spmv_load_halo<T, false>(a, hn, lane, fs, r, pold, qold, nxt);
       nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
     }
     const int q = k % kStages;
@@ -1374,7 +1375,7 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_co
     const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
     const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(pnew, o, P);
-    if (!a.zdirect) {  // publish the z faces for the neighbours
+    {  // publish the z faces for the neighbours
       T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
       zw[0] = P.v[0];
       zw[64] = P.v[7];
@@ -1417,7 +1418,7 @@ __device__ __forceinline__ void upd_load_own(const PcgArgs& a, int hw, int lane,
   ldcol(r, o, in.r);
 }
 
-template <typename T>
+template <typename T, bool ZD>
 __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane, const int fs[6],
                                               const T* p, int qcur, UpdIn<T>& in) {
   const HalfLeaf h = half_pos(hw, lane);
@@ -1431,7 +1432,7 @@ __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane
   }
   const int zs0 = fs[4], zs1 = fs[5];
   const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
-  if (a.zdirect) {
+  if constexpr (ZD) {
     in.zm = zv0 ? ldv(p + (unsigned(zs0) * 512u + unsigned(h.c) + 7u)) : T(0);
     in.zp = zv1 ? ldv(p + (unsigned(zs1) * 512u + unsigned(h.c))) : T(0);
     return;
@@ -1441,15 +1442,15 @@ __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane
   in.zp = zv1 ? ldv(zfp + unsigned(zs1) * 384u) : T(0);
 }
 
-template <typename T>
+template <typename T, bool ZD>
 __device__ __forceinline__ void upd_load(const PcgArgs& a, int hw, int lane, const int fs[6],
                                          const T* p, const T* x, const T* r, int qcur,
                                          UpdIn<T>& in) {
   upd_load_own<T>(a, hw, lane, p, x, r, in);
-  upd_load_halo<T>(a, hw, lane, fs, p, qcur, in);
+  upd_load_halo<T, ZD>(a, hw, lane, fs, p, qcur, in);
 }
 
-template <typename T, int DM>
+template <typename T, int DM, bool ZD>
 __global__ void __launch_bounds__(kHotThreads, 4)
     k_pcg_update_pl(const __grid_constant__ PcgArgs a) {
   __shared__ Tile<T> tiles[kHotThreads / 32];
@@ -1485,7 +1486,7 @@ __global__ void __launch_bounds__(kHotThreads, 4)
   if (hw < nhw) {
     const HalfLeaf h = half_pos(hw, lane);
     ldcol(p, unsigned(h.s) * 512u + unsigned(h.c), cur.P);
-    upd_load_halo<T>(a, hw, lane, fs, p, qcur, cur);
+    upd_load_halo<T, ZD>(a, hw, lane, fs, p, qcur, cur);
   }
   head_issue<DM, 1>(hs, a, kPartPAp);
   const HotHead head = update_head<DM>(hs, a);
@@ -1500,7 +1501,7 @@ __global__ void __launch_bounds__(kHotThreads, 4)
     if (hn < nhw) {
       int fs[6];
       face_slots(nbl, fs);
-      upd_load<T>(a, hn, lane, fs, p, x, r, qcur, nxt);
+      upd_load<T, ZD>(a, hn, lane, fs, p, x, r, qcur, nxt);
       nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
     }
     const HalfLeaf h = half_pos(hw, lane);
@@ -1521,7 +1522,7 @@ __global__ void __launch_bounds__(kHotThreads, 4)
     const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
     stcol(x, o, cur.x);
     stcol(r, o, cur.r);
-    if (!a.zdirect) {
+    if constexpr (!ZD) {
       T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + unsigned(h.fidx));
       zw[0] = cur.r.v[0];
       zw[64] = cur.r.v[7];
@@ -1928,21 +1929,34 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
 // FSIM_PCG_TMA=1), the register-pipelined pair (fp32 vectors), or the plain
 // pair (fp64 vectors, or FSIM_PCG_PIPE=0).
 template <typename T, int DM>
-void* spmv_kernel(const fsim_sim* s) {
+void* spmv_kernel(const fsim_sim* s, bool zd) {
   if constexpr (std::is_same<T, float>::value) {
     if constexpr (DM == 0) {
       if (s->use_pipe && s->use_tma) return reinterpret_cast<void*>(k_pcg_spmv_tma<DM>);
     }
-    if (s->use_pipe) return reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM>);
+    if (s->use_pipe)
+      return zd ? reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM, true>)
+                : reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM, false>);
   }
   return reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
 }
 template <typename T, int DM>
-void* update_kernel(const fsim_sim* s) {
+void* update_kernel(const fsim_sim* s, bool zd) {
   if constexpr (std::is_same<T, float>::value) {
-    if (s->use_pipe) return reinterpret_cast<void*>(k_pcg_update_pl<T, DM>);
+    if (s->use_pipe)
+      return zd ? reinterpret_cast<void*>(k_pcg_update_pl<T, DM, true>)
+                : reinterpret_cast<void*>(k_pcg_update_pl<T, DM, false>);
   }
   return reinterpret_cast<void*>(k_pcg_update<T, DM>);
+}
+// Large systems: the pipelined kernels read z-face neighbours from the
+// vectors (L2 hits) instead of the published planes, which no longer fit in
+// L2 and cost about 4 B of DRAM traffic per unknown and iteration.  The
+// spmv's bulk-copy variant always uses the planes.
+template <typename T>
+bool use_zdirect(const fsim_sim* s, int n_pleaf) {
+  return std::is_same<T, float>::value && s->use_pipe && !s->use_tma &&
+         (s->zdirect > 0 || (s->zdirect < 0 && n_pleaf > kZDirectLeaves));
 }
 int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
   fsim::ProfScope ps(s, name);
@@ -1992,7 +2006,8 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl) {
       kn.kernel.gridDim = dim3(unsigned(wgrid));
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
-      kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s) : spmv_kernel<T, DM>(s);
+      const bool zd = use_zdirect<T>(s, a.n_pleaf);
+      kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s, zd) : spmv_kernel<T, DM>(s, zd);
       cudaGraphEdgeData ed = {};
       if (pdl) {  // the successor may launch while this kernel's last CTAs finish
         ed.from_port = cudaGraphKernelNodePortProgrammatic;
@@ -2054,17 +2069,12 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   if (setup) FSIM_LAUNCH(s, nm_setup, (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
   const int wpb = kHotThreads / 32;
   int occ_a = 1, occ_b = 1;
-  void* const fn_spmv = spmv_kernel<T, DM>(s);
-  void* const fn_upd = update_kernel<T, DM>(s);
+  const bool zd = use_zdirect<T>(s, a.n_pleaf);
+  void* const fn_spmv = spmv_kernel<T, DM>(s, zd);
+  void* const fn_upd = update_kernel<T, DM>(s, zd);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, fn_spmv, kHotThreads, 0);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, fn_upd, kHotThreads, 0);
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
-  // Large systems: the pipelined kernels read z-face neighbours from the
-  // vectors (L2 hits) instead of the published planes, which no longer fit
-  // in L2 and cost about 4 B of DRAM traffic per unknown and iteration.
-  a.zdirect = (std::is_same<T, float>::value && s->use_pipe &&
-               (s->zdirect > 0 || (s->zdirect < 0 && a.n_pleaf > kZDirectLeaves)))
-                  ? 1 : 0;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks, kMaxHotGrid}));
   if (s->use_coop && !s->profiling) {
