@@ -782,16 +782,28 @@ int fsim_step_host(fsim_t* s, float dt, const fsim_pcg_params* prm, const float*
   }
   float* stage = s->part[s->cur ^ 1];
   float* outs[3] = {s->io_early_n == nl ? nullptr : out_pos, out_vel, out_gvel};
-  for (int f = 0; f < 3 && nl > 0; ++f) {
+  cudaError_t e = cudaSuccess;
+  for (int f = 0; f < 3 && nl > 0 && e == cudaSuccess; ++f) {
     if (!outs[f]) continue;
     float* sg = stage + size_t(f) * 3 * s->cap_p;
-    FSIM_LAUNCH(s, "soa_to_aos", k_soa_to_aos, unsigned((nl + 255) / 256), 256, 0,
-                s->part[s->cur], sg, nl, s->cap_p, 3 * f);
-    FSIM_CK(s, cudaMemcpyAsync(outs[f], sg, size_t(nl) * 12, cudaMemcpyDeviceToHost, s->stream));
+    {
+      fsim::ProfScope ps(s, "soa_to_aos");
+      k_soa_to_aos<<<unsigned((nl + 255) / 256), 256, 0, s->stream>>>(s->part[s->cur], sg, nl,
+                                                                     s->cap_p, 3 * f);
+      s->launches++;
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(outs[f], sg, size_t(nl) * 12, cudaMemcpyDeviceToHost, s->stream);
   }
-  FSIM_CK(s, cudaStreamSynchronize(s->stream));
-  FSIM_CK(s, cudaStreamSynchronize(s->io_stream));
+  // both streams finish before returning, also on an error: the early
+  // position copy writes into the caller's buffer
+  const cudaError_t e1 = cudaStreamSynchronize(s->stream);
+  const cudaError_t e2 = cudaStreamSynchronize(s->io_stream);
   s->io_early_n = -1;
+  if (e == cudaSuccess) e = e1;
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(s, e, "fsim_step_host download");
   return FSIM_OK;
 }
 
