@@ -10,7 +10,8 @@ value: steps/s with the particle state resident in HBM, CUDA events on the
 library's stream around exactly K steps (after W warm-up steps), max over
 ranks.  The particle state (32.2M particles, 1.16 GB) is larger than L2.
 e2e:   the same steps through the public C ABI from pinned host buffers:
-upload particles (H2D), step, download particles (D2H) every step.
+upload particles (H2D), step, download particles (D2H) every step; with the
+host link's measured bandwidth and the step time it allows (link_floor_ms).
 roofline: the dominant kernel's algorithmic bytes / its event-timed time.
 cpu_baseline: the oracle (a restatement of the reference CPU path, single
 thread, as the reference runs one partition with TBB at 1 thread) timed on
@@ -53,6 +54,12 @@ WORKLOADS = {
 #   pcg_update: read p_j, x, r (12) + flags (1); write x, r (8)       = 21 B
 ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update_mixed": 21,
              "pcg_spmv_f64": 25, "pcg_update_f64": 41}
+# The same iteration in the textbook formulation, where z = M^-1 r and Ap are stored:
+#   Ap = A p and p.Ap:                read p, flags; write Ap                 =  9 B
+#   x += a p; r -= a Ap; z; r.r, r.z: read x, p, r, Ap, flags; write x, r, z  = 29 B
+#   p = z + b p:                      read z, p; write p                      = 12 B
+# (fp32 vectors), keyed by the spmv kernel of the pair.
+UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50}
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
 # flushed before the launch) from one ncu capture of `bench.py --pcg-micro` on the 256^3
 # dam-break system (4.02 M unknowns); scaled by each step's unknowns.
@@ -289,6 +296,8 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / e2e_steps
     e2e_split["sequential_calls_ms"] = seq_ms
+    e2e_split.update(host_link_floor(hp, stream, device, ms / args.steps, kt,
+                                     max(1, min(args.steps, args.profile_steps))))
     barrier()
     ms, e2e_ms = max_over_ranks([ms, e2e_ms], device=f"cuda:{device}")
     sim.close()
@@ -298,6 +307,53 @@ def run_gpu(args, rank, world):
                 piters=piters, prows=prows, prof_ms=prof_ms,
                 n_particles=n_particles, n_fluid=n_fluid, e2e_ms=e2e_ms, e2e_split=e2e_split,
                 e2e_bytes=36 * n_particles)
+
+
+def host_link_floor(hp, stream, device, step_ms, kt, prof_steps):
+    """Host link bandwidth and the end-to-end floor it sets.
+
+    One particle array (12 B per particle, pinned) is copied each way, best
+    of 3, on the library's stream.  fsim_step_host needs all three arrays on
+    the device before the particle gather (P2G reads the velocities), and
+    can start the velocity and PIC-velocity downloads only after G2P; only
+    the advection/keying and the sort run while the uploads finish, and the
+    position download overlaps the rest of the step.  So no schedule beats
+        3 x upload + (device step - keys - sort) + 2 x download."""
+    import torch
+
+    flat = hp.reshape(-1)
+    dbuf = torch.empty(flat.numel(), dtype=flat.dtype, device=f"cuda:{device}")
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+
+    def best_ms(copy):
+        best = float("inf")
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                a.record(stream)
+                copy()
+                b.record(stream)
+                torch.cuda.synchronize()
+                best = min(best, a.elapsed_time(b))
+        return best
+
+    # blocking copies: a non-blocking one would leave an event of the library's
+    # stream on the pinned block, which outlives the stream
+    up = best_ms(lambda: dbuf.copy_(flat))
+    down = best_ms(lambda: flat.copy_(dbuf))
+    del dbuf
+    nbytes = flat.numel() * flat.element_size()
+    early = sum(kt[k][0] for k in ("advect_keys", "radix_sort(cub)") if k in kt) / prof_steps
+    return {"link_h2d_gbs": nbytes / (up * 1e-3) / 1e9,
+            "link_d2h_gbs": nbytes / (down * 1e-3) / 1e9,
+            "link_floor_ms": e2e_floor_ms(up, down, step_ms, early)}
+
+
+def e2e_floor_ms(up_ms, down_ms, step_ms, early_ms):
+    """Critical path of fsim_step_host given one array's upload and download
+    times: all three uploads, the step less the work that overlaps them,
+    then the two downloads that follow G2P."""
+    return 3 * up_ms + max(0.0, step_ms - early_ms) + 2 * down_ms
 
 
 def roofline(res):
@@ -331,6 +387,11 @@ def roofline(res):
                    us_per_iteration=loop * 1e3 / max(sum(its), 1), working_launches=sum(its),
                    share_of_step=loop / res["ms"] if res["ms"] > 0 else None,
                    time_source="fsim_pcg_stats.loop_ms: CUDA events on the library stream, timed steps")
+        if names[0] in UNFUSED_BYTES:
+            # the same loop time, counted in the textbook formulation's bytes
+            ub = UNFUSED_BYTES[names[0]]
+            out["unfused_alg_bytes_per_unknown"] = ub
+            out["unfused_frac"] = achieved * ub / per / peak
         if all(k in NCU_TRAFFIC_PER_UNKNOWN for k in names):
             out["traffic"] = sum(NCU_TRAFFIC_PER_UNKNOWN[k] for k in names) * n_rows
             out["traffic_source"] = "ncu capture of the 256^3 system (spmv + update), scaled by unknowns"
@@ -486,7 +547,7 @@ def pcg_compare(args):
     out["fastest_fp64_at_1e-6"] = bd
     out["speedup_mixed_vs_fp32"] = (bf["ms"] / bm["ms"]) if (bf and bm) else None
     out["speedup_mixed_vs_fp64"] = (bd["ms"] / bm["ms"]) if (bd and bm) else None
-    print(json.dumps(out))
+    print(json.dumps(out), flush=True)
     sim.close()
 
 
@@ -530,7 +591,7 @@ def pcg_micro(args):
         sim.synchronize()
         out[name + "_graph_us_per_iteration"] = round((time.perf_counter() - t0) / k * 1e6, 2)
     out["pcg_graph_mode"] = os.environ.get("FSIM_PCG_GRAPH", "1")
-    print(json.dumps(out))
+    print(json.dumps(out), flush=True)
     sim.close()
 
 
@@ -591,7 +652,7 @@ def adjoint_check(args):
            "grad_rel_l2_fp32_vs_fp64": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
            "seconds": {"scene": t_case, "forward": t_fwd, "backward": t_bwd, "fd": t_fd},
            "rows": rows}
-    print(json.dumps(out))
+    print(json.dumps(out), flush=True)
     ro.close()
     sim.close()
 
@@ -668,7 +729,7 @@ def main():
                                            f"path, one thread (one partition, TBB at 1 thread)"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(line), flush=True)
         return
 
     if world > 1:
@@ -699,7 +760,7 @@ def main():
                                 "kind": "port",
                                 "sample": f"first step of {args.workload} ({npart} particles), "
                                           f"stages timed on one thread; {how}"}
-    print(json.dumps(line))
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

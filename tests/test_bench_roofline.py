@@ -32,6 +32,8 @@ def test_pcg_pair_is_one_iteration():
                + bench.NCU_TRAFFIC_PER_UNKNOWN["pcg_update"]) * 4_050_000
     assert r["traffic"] == pytest.approx(traffic)
     assert set(r["per_kernel_profiled"]) == {"pcg_spmv", "pcg_update"}
+    assert r["unfused_alg_bytes_per_unknown"] == 50
+    assert r["unfused_frac"] == pytest.approx(r["frac"] * 50 / 34)
 
 
 def test_mixed_pair_and_other_kernels():
@@ -47,3 +49,11 @@ def test_mixed_pair_and_other_kernels():
 
 def test_whole_job_rate_counts_every_replica():
     assert bench.whole_job_rate(4, 20, 1000.0) == pytest.approx(80.0)
+
+
+def test_e2e_floor():
+    # 386 MB arrays at 211 / 193 GB/s, a 29.9 ms step of which 1.13 ms overlaps the uploads
+    up, down = 386e6 / 211e9 * 1e3, 386e6 / 193e9 * 1e3
+    f = bench.e2e_floor_ms(up, down, 29.9, 1.13)
+    assert f == pytest.approx(3 * up + 28.77 + 2 * down)
+    assert bench.e2e_floor_ms(1.0, 1.0, 0.5, 2.0) == pytest.approx(5.0)
