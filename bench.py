@@ -165,7 +165,7 @@ def make_sim(wl, args, device):
 
     n = wl["n"]
     g, f = fsim.physical_gravity(n)
-    sim = fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8, device=device)
+    sim = fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, args.ppc, device=device)
     sim.seed(fsim.scene_passes(wl["scene"], n), seed=0)
     return sim
 
@@ -685,12 +685,17 @@ def main():
     ap.add_argument("--pcg-micro", action="store_true",
                     help="per-kernel PCG times on one step's system (fixed iteration count)")
     ap.add_argument("--micro-iters", type=int, default=300)
+    ap.add_argument("--ppc", type=int, default=8,
+                    help="particles per fluid cell (8 defines the workloads; fewer gives the same "
+                         "pressure system in less memory, for --pcg-micro captures only)")
     ap.add_argument("--lib", default=None, help="path of a variant libfsim.so (A/B runs)")
     ap.add_argument("--adjoint-check", action="store_true",
                     help="differentiable rollout: adjoint vs central differences")
     ap.add_argument("--adjoint-n", type=int, default=128)
     ap.add_argument("--adjoint-dirs", type=int, default=32)
     args = ap.parse_args()
+    if args.ppc != 8 and not args.pcg_micro:
+        ap.error("--ppc changes the workload: it is for --pcg-micro only")
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

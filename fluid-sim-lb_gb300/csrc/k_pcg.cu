@@ -425,28 +425,82 @@ __device__ __forceinline__ V ldv(const V* p) {
 #endif
 }
 
+// Column offsets are multiples of 8 cells, so a float column starts 32-byte
+// aligned: it moves as one 256-bit access per lane (sm_100 and later).  Two
+// 128-bit accesses would each touch every 128-byte line of the half leaf, so
+// the L1 pipeline would see each line twice.
+#ifndef FSIM_PCG_COL256
+#define FSIM_PCG_COL256 1
+#endif
+__device__ __forceinline__ void unpack2(unsigned long long u, float& lo, float& hi) {
+  lo = __uint_as_float(unsigned(u));
+  hi = __uint_as_float(unsigned(u >> 32));
+}
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+  return (static_cast<unsigned long long>(__float_as_uint(hi)) << 32) | __float_as_uint(lo);
+}
 __device__ __forceinline__ void ldcol(const float* __restrict__ p, int64_t o, Col<float>& c) {
+#if FSIM_PCG_COL256 && !FSIM_PCG_LDCG
+  const ulonglong4_32a a = *reinterpret_cast<const ulonglong4_32a*>(p + o);
+  unpack2(a.x, c.v[0], c.v[1]);
+  unpack2(a.y, c.v[2], c.v[3]);
+  unpack2(a.z, c.v[4], c.v[5]);
+  unpack2(a.w, c.v[6], c.v[7]);
+#else
   const float4 a = ldv(reinterpret_cast<const float4*>(p + o));
   const float4 b = ldv(reinterpret_cast<const float4*>(p + o + 4));
   c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
   c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
+#endif
 }
 __device__ __forceinline__ void ldcol(const double* __restrict__ p, int64_t o, Col<double>& c) {
+#if FSIM_PCG_COL256 && !FSIM_PCG_LDCG
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double4_32a a = *reinterpret_cast<const double4_32a*>(p + o + 4 * k);
+    c.v[4 * k] = a.x;
+    c.v[4 * k + 1] = a.y;
+    c.v[4 * k + 2] = a.z;
+    c.v[4 * k + 3] = a.w;
+  }
+#else
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const double2 a = ldv(reinterpret_cast<const double2*>(p + o + 2 * k));
     c.v[2 * k] = a.x;
     c.v[2 * k + 1] = a.y;
   }
+#endif
 }
 __device__ __forceinline__ void stcol(float* __restrict__ p, int64_t o, const Col<float>& c) {
+#if FSIM_PCG_COL256
+  ulonglong4_32a a;
+  a.x = pack2(c.v[0], c.v[1]);
+  a.y = pack2(c.v[2], c.v[3]);
+  a.z = pack2(c.v[4], c.v[5]);
+  a.w = pack2(c.v[6], c.v[7]);
+  *reinterpret_cast<ulonglong4_32a*>(p + o) = a;
+#else
   *reinterpret_cast<float4*>(p + o) = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
   *reinterpret_cast<float4*>(p + o + 4) = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
+#endif
 }
 __device__ __forceinline__ void stcol(double* __restrict__ p, int64_t o, const Col<double>& c) {
+#if FSIM_PCG_COL256
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    double4_32a a;
+    a.x = c.v[4 * k];
+    a.y = c.v[4 * k + 1];
+    a.z = c.v[4 * k + 2];
+    a.w = c.v[4 * k + 3];
+    *reinterpret_cast<double4_32a*>(p + o + 4 * k) = a;
+  }
+#else
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     *reinterpret_cast<double2*>(p + o + 2 * k) = make_double2(c.v[2 * k], c.v[2 * k + 1]);
+#endif
 }
 // L2-only column load (data another CTA wrote earlier in the same launch)
 __device__ __forceinline__ void ldcol_cg(const float* p, int64_t o, Col<float>& c) {
