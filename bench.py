@@ -63,7 +63,7 @@ UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50}
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
 # flushed before the launch) from one ncu capture of `bench.py --pcg-micro` on the 256^3
 # dam-break system (4.02 M unknowns); scaled by each step's unknowns.
-NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.89e6 / 4021250, "pcg_update": 61.23e6 / 4021250}
+NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.94e6 / 4021250, "pcg_update": 61.35e6 / 4021250}
 # The two launches of one PCG iteration (spmv then update) are reported as one unit: the
 # split of the iteration's work between them is a design choice (the update could take
 # x += alpha p or leave it), and their times are nearly equal.
