@@ -125,10 +125,58 @@ __global__ void k_keys(float* __restrict__ part, int64_t cap, const uint32_t* __
   }
 }
 
+// Live particles = index of the first dead key: the keys are sorted and the
+// dead key is the largest value.  One block narrows [lo, hi] (which holds
+// that index; hi = n when no key is dead) by probing blockDim.x evenly spaced
+// keys per round, about 1000x per round, instead of reading all n keys.
 __global__ void k_count_live(const uint32_t* __restrict__ k, int64_t n, int64_t* cnt) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (k[i] != kDeadKey && (i + 1 == n || k[i + 1] == kDeadKey)) cnt[0] = i + 1;
+  __shared__ int64_t s_lo, s_hi;
+  __shared__ int s_first;
+  if (threadIdx.x == 0) {
+    s_lo = 0;
+    s_hi = n;
+  }
+  __syncthreads();
+  for (;;) {
+    const int64_t lo = s_lo, hi = s_hi;
+    if (lo >= hi) break;
+    const int64_t nb = blockDim.x;
+    const int64_t step = (hi - lo + nb - 1) / nb;
+    const int64_t pr = lo + int64_t(threadIdx.x) * step;  // this thread's probe
+    if (threadIdx.x == 0) s_first = INT_MAX;
+    __syncthreads();
+    if (pr < hi && k[pr] == kDeadKey) atomicMin(&s_first, int(threadIdx.x));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int t = s_first;
+      if (t == INT_MAX) {  // every probe live: the first dead key lies past the last probe
+        const int64_t last = lo + ((hi - 1 - lo) / step) * step;
+        s_lo = last + 1;
+      } else {  // between the last live probe and probe t (dead)
+        s_lo = t == 0 ? lo : lo + int64_t(t - 1) * step + 1;
+        s_hi = lo + int64_t(t) * step;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cnt[0] = s_lo;
+}
+
+// Four sorted keys per thread (one 16-byte load; key arrays start 256-byte
+// aligned), so a warp streams 512 contiguous bytes per request.
+constexpr int kKeysPerThread = 4;
+__device__ __forceinline__ void load_keys4(const uint32_t* __restrict__ k, int64_t i0, int64_t n,
+                                           uint32_t (&v)[kKeysPerThread]) {
+  if (i0 + kKeysPerThread <= n) {
+    const uint4 q = *reinterpret_cast<const uint4*>(k + i0);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  } else {
+#pragma unroll
+    for (int j = 0; j < kKeysPerThread; ++j) v[j] = i0 + j < n ? k[i0 + j] : kDeadKey;
+  }
 }
 
 __global__ void k_gather(const float* __restrict__ in, float* __restrict__ out, int64_t cap,
@@ -143,10 +191,19 @@ __global__ void k_gather(const float* __restrict__ in, float* __restrict__ out, 
 
 __global__ void k_mark_pleaf(const uint32_t* __restrict__ k, const int64_t* __restrict__ cnt,
                              uint8_t* __restrict__ flag) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= cnt[0]) return;
-  uint32_t l = k[i] >> 9;
-  if (i == 0 || (k[i - 1] >> 9) != l) flag[l] = 1;
+  const int64_t n = cnt[0];
+  const int64_t i0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kKeysPerThread;
+  if (i0 >= n) return;
+  uint32_t v[kKeysPerThread];
+  load_keys4(k, i0, n, v);
+  uint32_t prev = i0 == 0 ? kDeadKey : (k[i0 - 1] >> 9);  // kDeadKey is no leaf id
+#pragma unroll
+  for (int j = 0; j < kKeysPerThread; ++j) {
+    if (i0 + j >= n) break;
+    const uint32_t l = v[j] >> 9;
+    if (l != prev) flag[l] = 1;
+    prev = l;
+  }
 }
 
 __global__ void k_dilate(uint8_t* __restrict__ flag, LeafMap lm) {
@@ -211,16 +268,34 @@ __global__ void k_nbr(const int32_t* __restrict__ leaf_of, const int32_t* __rest
 __global__ void k_ranges(const uint32_t* __restrict__ k, const int64_t* __restrict__ cnt,
                          const int32_t* __restrict__ slot, uint2* __restrict__ cr,
                          uint2* __restrict__ lr) {
-  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t n = cnt[0];
-  if (i >= n) return;
-  const uint32_t key = k[i];
-  const int s = slot[key >> 9];
-  uint2* c = &cr[int64_t(s) * 512 + (key & 511u)];
-  if (i == 0 || k[i - 1] != key) c->x = uint32_t(i);
-  if (i + 1 == n || k[i + 1] != key) c->y = uint32_t(i + 1);
-  if (i == 0 || (k[i - 1] >> 9) != (key >> 9)) lr[s].x = uint32_t(i);
-  if (i + 1 == n || (k[i + 1] >> 9) != (key >> 9)) lr[s].y = uint32_t(i + 1);
+  const int64_t i0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kKeysPerThread;
+  if (i0 >= n) return;
+  uint32_t v[kKeysPerThread + 2];  // the key before, the four keys, the key after
+  {
+    uint32_t q[kKeysPerThread];
+    load_keys4(k, i0, n, q);
+#pragma unroll
+    for (int j = 0; j < kKeysPerThread; ++j) v[j + 1] = q[j];
+  }
+  v[0] = i0 == 0 ? kDeadKey : k[i0 - 1];  // kDeadKey: no live key equals it
+  v[kKeysPerThread + 1] = i0 + kKeysPerThread < n ? k[i0 + kKeysPerThread] : kDeadKey;
+#pragma unroll
+  for (int j = 0; j < kKeysPerThread; ++j) {
+    const int64_t i = i0 + j;
+    if (i >= n) break;
+    const uint32_t key = v[j + 1];
+    // past the last live key, v holds kDeadKey, which ends every range
+    const uint32_t before = v[j], after = v[j + 2];
+    const bool cell_start = before != key, cell_end = after != key;
+    if (!(cell_start || cell_end)) continue;
+    const int s = slot[key >> 9];
+    uint2* c = &cr[int64_t(s) * 512 + (key & 511u)];
+    if (cell_start) c->x = uint32_t(i);
+    if (cell_end) c->y = uint32_t(i + 1);
+    if (cell_start && (before >> 9) != (key >> 9)) lr[s].x = uint32_t(i);
+    if (cell_end && (after >> 9) != (key >> 9)) lr[s].y = uint32_t(i + 1);
+  }
 }
 
 // ---- seeding (FlipSimulation::InitializePhiAndParticles restated) -------
@@ -528,7 +603,7 @@ int rebuild_topology(fsim_sim* s) {
 int rebuild_after_sort(fsim_sim* s, bool gather) {
   const int64_t n = s->n_total;
   FSIM_CK(s, cudaMemsetAsync(s->d_cnt, 0, 3 * sizeof(int64_t), s->stream));
-  FSIM_LAUNCH(s, "count_live", k_count_live, nblk(n, 256), 256, 0, s->keys[0], n, s->d_cnt);
+  FSIM_LAUNCH(s, "count_live", k_count_live, 1, 1024, 0, s->keys[0], n, s->d_cnt);
   if (gather) {
     // a velocity upload still in flight on the I/O stream (fsim_step_host)
     if (s->io_vel_pending) {
@@ -542,7 +617,7 @@ int rebuild_after_sort(fsim_sim* s, bool gather) {
   // leaves
   const uint32_t D = s->lm.dense;
   FSIM_CK(s, cudaMemsetAsync(s->d_flag, 0, D, s->stream));
-  FSIM_LAUNCH(s, "mark_leaves", k_mark_pleaf, nblk(n, 256), 256, 0, s->keys[0], s->d_cnt,
+  FSIM_LAUNCH(s, "mark_leaves", k_mark_pleaf, nblk(n, 256 * kKeysPerThread), 256, 0, s->keys[0], s->d_cnt,
               s->d_flag);
   FSIM_LAUNCH(s, "dilate_leaves", k_dilate, nblk(D, 256), 256, 0, s->d_flag, s->lm);
   FSIM_LAUNCH(s, "scan_input", k_scan_in, nblk(D, 256), 256, 0, s->d_flag, s->d_scan, D);
@@ -578,7 +653,7 @@ int rebuild_after_sort(fsim_sim* s, bool gather) {
                                s->stream));
     FSIM_CK(s, cudaMemsetAsync(s->d_leaf_range, 0, size_t(s->n_pleaf) * sizeof(uint2), s->stream));
   }
-  FSIM_LAUNCH(s, "cell_ranges", k_ranges, nblk(s->n_live, 256), 256, 0, s->keys[0], s->d_cnt,
+  FSIM_LAUNCH(s, "cell_ranges", k_ranges, nblk(s->n_live, 256 * kKeysPerThread), 256, 0, s->keys[0], s->d_cnt,
               s->d_slot, s->d_cell_range, s->d_leaf_range);
   s->have_topology = true;
   s->deleted_outside = false;
