@@ -1,13 +1,15 @@
 // k_grid.cu -- grid stages of the FLIP step on the sparse 8^3 brick layout.
 //
 // P2G (FlipSimulation::TransferParticlesToGrid, common/flip_simulation.cc:
-// 809-923, with ScatterWeight<D> :927-1009) runs one CTA per grid leaf.  The
-// CTA walks the 10^3 cells whose particles can reach its 8^3 nodes (the same
-// halo the reference buffers per leaf), splats every particle's trilinear
-// MAC weights into shared-memory accumulators for the nodes it owns, and
-// then writes each node exactly once: no global atomics, no halo write-back.
-// The fused variant folds the rest of the per-node work of the step into
-// that write: normalisation with the 1e-5 cut, ApplyBoundaryConditions,
+// 809-923, with ScatterWeight<D> :927-1009) runs in two passes, each particle
+// visited once.  Pass 1 (one CTA per particle leaf) splats the leaf's
+// particles into a 10^3 node block (the leaf's nodes and the layer around
+// them, the halo the reference buffers per leaf) in shared-memory fixed-point
+// accumulators and writes the block out.  Pass 2 (one CTA per grid leaf)
+// sums, per node, its own block entry and the neighbour blocks that cover it,
+// and writes each node exactly once: no global atomics.  The fused pass 2
+// folds the rest of the per-node work of the step into that write:
+// normalisation with the 1e-5 cut, ApplyBoundaryConditions,
 // SaveGridVelocities, AddGravity and the second ApplyBoundaryConditions.
 //
 // The remaining kernels restate ComputeDivergence (:716-736),
