@@ -23,9 +23,11 @@
 // HBM bytes per unknown per iteration: spmv reads r, p_{j-1}, flags and
 // writes p_j (13 B); update reads p_j, x, r, flags and writes x, r (21 B).
 // Each warp owns half a leaf: a lane holds one z-column of 8 cells in
-// registers, neighbours come from warp shuffles and only the faces of the
-// half leaf are read from memory.  Kernels launched after the stop flag is set return at
-// once, so the host polls the flag only between chunks of iterations.
+// registers (loaded and stored as one 256-bit access), the x/y neighbour
+// columns come from a per-warp shared tile, and only the faces of the half
+// leaf are read from memory besides.  The iterations run as a CUDA graph
+// whose conditional WHILE node stops on the device-side loop test; kernels
+// launched after the stop flag is set return at once.
 //
 // Precision modes: FP32 (reference: fp32 vectors, fp32 dots), MIXED (fp32
 // vectors, dots accumulated exactly: FMA error-free products and
@@ -400,19 +402,18 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
 // ---- column-blocked leaf access -------------------------------------------
 // One warp owns half of an 8^3 leaf (x in [0,4) or [4,8)).  Lane L owns the
 // z-column (xb + (L>>3), L&7); a column is 8 contiguous cells (offset
-// x*64 + y*8, 32 B of floats), so the z-neighbours are registers, the
-// y-neighbours are lanes L-1 / L+1 and the x-neighbours lanes L-8 / L+8 --
-// warp shuffles.  Only the faces of the half leaf are read from memory (the
-// other half's boundary plane like a neighbour face).  No shared memory and
-// no CTA barrier in the hot loop.
+// x*64 + y*8, 32 B of floats), so the z-neighbours are registers.  The x/y
+// neighbour columns go through a per-warp shared tile (below); the columns
+// just outside the half leaf (the other half's boundary plane like a
+// neighbour face) are each loaded by one lane.  No CTA barrier in the hot
+// loop: a warp synchronises only itself around the tile.
 template <typename T>
 struct Col {
   T v[8];
 };
 
-// Column loads: a lane reads its 32 B column as two 16 B vectors.  With the
-// default (L1-allocating) load the second vector hits the line the first
-// brought in; FSIM_PCG_LDCG=1 selects L2-only loads instead.
+// Column loads of the 128-bit form (FSIM_PCG_COL256=0): a lane reads its 32 B
+// column as two 16 B vectors; FSIM_PCG_LDCG=1 makes them L2-only.
 #ifndef FSIM_PCG_LDCG
 #define FSIM_PCG_LDCG 0
 #endif
