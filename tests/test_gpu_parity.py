@@ -80,6 +80,40 @@ def test_move_particles_bitexact(cfg):
     sim.close()
 
 
+@pytest.mark.parametrize("count", [1, 3, 4, 5, 9, 1027])
+def test_move_particles_ragged_and_all_deleted(count):
+    """Particle counts that are not a multiple of the four keys a thread of
+    the rebinning kernels takes: positions and leaves bit-exact with the
+    oracle.  Then every particle is put on x = N, where the move clamps it
+    into the wall cell N and deletes it: no live particle and no leaf remain,
+    and the empty state still steps."""
+    n = 16
+    orc = make_oracle(n, "dam_break")
+    rng = np.random.default_rng(count)
+    pos = rng.uniform(0.0, float(n), (count, 3)).astype(np.float32)
+    vel = rng.normal(0.0, 3.0 * n, (count, 3)).astype(np.float32)
+    orc.set_particles(pos, vel, vel.copy())
+    sim = make_gpu(orc)
+    sim.move_particles(0.01)
+    orc.move_particles(0.01)
+    p1, v1, _ = sim.download_particles()
+    p0, v0, _ = orc.particles()
+    assert np.array_equal(p1, p0) and np.array_equal(v1, v0)
+    assert np.array_equal(sim.leaves(), orc.leaves())
+    wall = p0.copy()
+    wall[:, 0] = float(n)
+    z = np.zeros_like(wall)
+    orc.set_particles(wall, z, z.copy())
+    sim.upload_particles(wall, z, z.copy())
+    sim.move_particles(0.01)
+    orc.move_particles(0.01)
+    assert sim.particle_count() == 0 == orc.particles()[0].shape[0]
+    assert np.array_equal(sim.leaves(), orc.leaves())
+    st = sim.step(0.004, fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 100, tolerance=1e-5))
+    assert st.particles == 0 and sim.particle_count() == 0
+    sim.close()
+
+
 def _stagewise(cfg, dt=0.01):
     n = cfg["n"]
     orc = make_oracle(n, cfg["scene"], cfg["boundary"], cfg["solids"], noise=_noise(n))
