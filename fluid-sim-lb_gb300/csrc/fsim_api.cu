@@ -819,9 +819,15 @@ int fsim_step(fsim_t* s, float dt, const fsim_pcg_params* prm, fsim_step_stats* 
     s->delete_in_sources = true;
     s->src_time = t;
   }
-  // MoveParticles + DeleteParticlesInSolids
+  // MoveParticles + DeleteParticlesInSolids.  The rebinning gather leaves
+  // gvel behind: G2P below rewrites it for every live particle, and nothing
+  // reads it before.  Not under the tank boundary, whose deletions after P2G
+  // leave dead particles that G2P skips.
   if ((rc = launch_keys_from_positions(s, 1, dt))) return rc;
-  if ((rc = rebuild_topology(s))) return rc;
+  s->gather_skip_gvel = s->cfg.boundary != FSIM_BOUNDARY_TANK;
+  rc = rebuild_topology(s);
+  s->gather_skip_gvel = false;
+  if (rc) return rc;
   if (s->io_early_pos && (rc = start_early_position_download(s))) return rc;
   reset_grid_flags(s);
   // TransferParticlesToGrid + BC + SaveGridVelocities + AddGravity + BC

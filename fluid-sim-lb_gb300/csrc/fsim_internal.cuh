@@ -200,6 +200,9 @@ struct fsim_sim {
   float* io_stage = nullptr;   // AoS staging of the early position download
   int64_t io_stage_cap = 0;
   bool io_vel_pending = false; // vel upload in flight on io_stream (ev_io)
+  // fsim_step: the rebinning gather moves pos and vel only; G2P rewrites
+  // gvel for every live particle before anything reads it again
+  bool gather_skip_gvel = false;
   float* io_early_pos = nullptr;  // host destination of the early position download
   int64_t io_early_cap = 0;
   int64_t io_early_n = -1;     // particles the early download copied (-1: none)

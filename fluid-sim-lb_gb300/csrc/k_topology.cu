@@ -179,6 +179,8 @@ __device__ __forceinline__ void load_keys4(const uint32_t* __restrict__ k, int64
   }
 }
 
+// Permutes the first NF particle arrays (9: pos, vel, gvel; 6: pos, vel).
+template <int NF>
 __global__ void k_gather(const float* __restrict__ in, float* __restrict__ out, int64_t cap,
                          const uint32_t* __restrict__ perm, const int64_t* __restrict__ cnt) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -186,7 +188,7 @@ __global__ void k_gather(const float* __restrict__ in, float* __restrict__ out, 
   if (i >= n) return;
   const int64_t src = perm[i];
 #pragma unroll
-  for (int f = 0; f < 9; ++f) out[f * cap + i] = in[f * cap + src];
+  for (int f = 0; f < NF; ++f) out[f * cap + i] = in[f * cap + src];
 }
 
 __global__ void k_mark_pleaf(const uint32_t* __restrict__ k, const int64_t* __restrict__ cnt,
@@ -610,8 +612,13 @@ int rebuild_after_sort(fsim_sim* s, bool gather) {
       FSIM_CK(s, cudaStreamWaitEvent(s->stream, s->ev_io, 0));
       s->io_vel_pending = false;
     }
-    FSIM_LAUNCH(s, "gather_particles", k_gather, nblk(n, 256), 256, 0, s->part[s->cur],
-                s->part[s->cur ^ 1], s->cap_p, s->vals[0], s->d_cnt);
+    if (s->gather_skip_gvel) {
+      FSIM_LAUNCH(s, "gather_particles", k_gather<6>, nblk(n, 256), 256, 0, s->part[s->cur],
+                  s->part[s->cur ^ 1], s->cap_p, s->vals[0], s->d_cnt);
+    } else {
+      FSIM_LAUNCH(s, "gather_particles", k_gather<9>, nblk(n, 256), 256, 0, s->part[s->cur],
+                  s->part[s->cur ^ 1], s->cap_p, s->vals[0], s->d_cnt);
+    }
     s->cur ^= 1;
   }
   // leaves

@@ -294,7 +294,10 @@ typedef struct fsim_step_stats {
  * DeleteOutsideParticles, ReinitializePhiSimple, AddGravity(dt),
  * ApplyBoundaryConditions, ComputeDivergence, PCG solve,
  * UpdateVelocityFromPressure, GetVelocityUpdate, UpdateParticlesFromGrid --
- * run as fused device kernels.  stats may be NULL. */
+ * run as fused device kernels.  stats may be NULL.  A step that fails after
+ * the rebinning leaves the particles' PIC velocities (gvel) undefined: the
+ * rebinning moves them only for the per-stage calls, since the step's G2P
+ * rewrites them. */
 int fsim_step(fsim_t* sim, float dt, const fsim_pcg_params* params,
               fsim_step_stats* stats);
 /* One step on a host-resident particle state: the same results as
