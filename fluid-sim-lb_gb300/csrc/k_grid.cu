@@ -107,6 +107,21 @@ __device__ __forceinline__ int node_index(int li, int lj, int lk) {
   return ((li + 1) * 10 + (lj + 1)) * 10 + (lk + 1);
 }
 
+// Bits t = (i * e1 + j) * e2 + k of a component-D box (extent 2 on axis D,
+// 3 on the others) whose coordinate on axis ax is in the position set m.
+// A particle reaches the box nodes in the AND of its per-axis sets.
+__host__ __device__ constexpr unsigned box_axis_mask(int D, int ax, unsigned m) {
+  unsigned r = 0u;
+  const int e0 = D == 0 ? 2 : 3, e1 = D == 1 ? 2 : 3, e2 = D == 2 ? 2 : 3;
+  for (int i = 0; i < e0; ++i)
+    for (int j = 0; j < e1; ++j)
+      for (int k = 0; k < e2; ++k) {
+        const int c = ax == 0 ? i : (ax == 1 ? j : k);
+        if ((m >> c) & 1u) r |= 1u << ((i * e1 + j) * e2 + k);
+      }
+  return r;
+}
+
 __global__ void __launch_bounds__(256) k_p2g_cells(const __grid_constant__ GridArgs a) {
   __shared__ unsigned long long sv[3][kNodeBlock];
   __shared__ unsigned long long sw[3][kNodeBlock];
@@ -177,10 +192,16 @@ __global__ void __launch_bounds__(256) k_p2g_cells(const __grid_constant__ GridA
               const float ww = __fmul_rn(wij, w1[2][k]);
               am[t] = __fadd_rn(am[t], __fmul_rn(ww, uD));
               aw[t] = __fadd_rn(aw[t], ww);
-              if (((m1[0] >> i) & (m1[1] >> j) & (m1[2] >> k)) & 1u) reach |= 1u << t;
             }
           }
         }
+        unsigned rp = box_axis_mask(D, D, 3u);  // every position on the normal axis
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          if (ax == D) continue;
+          rp &= m1[ax] == 3u ? box_axis_mask(D, ax, 3u) : box_axis_mask(D, ax, 6u);
+        }
+        reach |= rp;
       }
       // flush the reached box nodes (local coordinates -1..8)
       const int b0 = cl[0] - (D == 0 ? 0 : 1), b1 = cl[1] - (D == 1 ? 0 : 1),
