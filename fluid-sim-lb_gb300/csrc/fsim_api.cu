@@ -190,8 +190,10 @@ int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf) {
     if ((rc = dmalloc(s, &s->d_nbr, size_t(cap) * 27))) return rc;
     s->cap_leaf = cap;
   }
-  if (n_pleaf > s->cap_pleaf) {
-    int64_t cap = std::min<int64_t>(int64_t(s->lm.dense), std::max<int64_t>(n_pleaf * 5 / 4, 64));
+  // one slot past the particle leaves: the PCG's zeroed null slot
+  if (n_pleaf + 1 > s->cap_pleaf) {
+    int64_t cap = std::min<int64_t>(int64_t(s->lm.dense) + 1,
+                                    std::max<int64_t>((int64_t(n_pleaf) + 1) * 5 / 4, 64));
     dfree(s->d_cell_range); dfree(s->d_leaf_range);
     dfree(s->div); dfree(s->pres); dfree(s->r); dfree(s->p[0]); dfree(s->p[1]); dfree(s->Ap);
     dfree(s->flags); dfree(s->x64); dfree(s->r64); dfree(s->p64[0]); dfree(s->p64[1]);

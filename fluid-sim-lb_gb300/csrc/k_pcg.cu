@@ -39,6 +39,12 @@
 
 #include "fsim_internal.cuh"
 
+// Halo and z-face loads of missing neighbours read a zeroed null slot (see
+// slot_or_null); 0 restores the validity branches.
+#ifndef FSIM_PCG_NULLSLOT
+#define FSIM_PCG_NULLSLOT 1
+#endif
+
 namespace fsim {
 
 namespace {
@@ -321,6 +327,21 @@ template <typename T, int DM>
 __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ PcgArgs a) {
   T* x = static_cast<T*>(a.x);
   T* r = static_cast<T*>(a.r);
+#if FSIM_PCG_NULLSLOT
+  if (std::is_same<T, float>::value && blockIdx.x == gridDim.x - 1) {
+    // the null slot n_pleaf read by the pipelined kernels' halo loads
+    const int64_t o = int64_t(a.n_pleaf) * 512;
+    for (int v = threadIdx.x; v < 512; v += kThreads) {
+      a.flags[o + v] = 0;
+      r[o + v] = T(0);
+      static_cast<T*>(a.p0)[o + v] = T(0);
+      static_cast<T*>(a.p1)[o + v] = T(0);
+    }
+    for (int v = threadIdx.x; v < 384; v += kThreads)
+      static_cast<T*>(a.zf)[int64_t(a.n_pleaf) * 384 + v] = T(0);
+    for (int v = threadIdx.x; v < 128; v += kThreads) a.zff[int64_t(a.n_pleaf) * 128 + v] = 0;
+  }
+#endif
   Dot<DM> drr, drz, dbb;
   int nfluid = 0;
   for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
@@ -1134,6 +1155,15 @@ __device__ __forceinline__ void spmv_load_own(const PcgArgs& a, int hw, int lane
 // ... and the halo column and z faces, addressed through the face slots.
 // ZD: z-face neighbours read from the vectors (large systems) instead of the
 // published planes.
+//
+// FSIM_PCG_NULLSLOT: a missing neighbour (no leaf, or a leaf without PCG
+// unknowns) reads slot n_pleaf instead, which the setup zeroes (flags, r,
+// both p and their z-face planes) and no kernel writes during the solve, so
+// the loads need no validity branch.  The particle-leaf capacity keeps that
+// slot.
+__device__ __forceinline__ unsigned slot_or_null(int slot, int n_pleaf) {
+  return unsigned(slot >= 0 && slot < n_pleaf ? slot : n_pleaf);
+}
 template <typename T, bool ZD>
 __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lane, const int fs[6],
                                                const T* r, const T* pold, int qold,
@@ -1141,6 +1171,34 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   const HalfLeaf h = half_pos(hw, lane);
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
+#if FSIM_PCG_NULLSLOT
+  if constexpr (std::is_same<T, float>::value) {
+    const unsigned hb = slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox);
+    in.hf = ldflags(a.flags, hb);
+    ldcol(r, hb, in.hr);
+    ldcol(pold, hb, in.hp);
+    const unsigned z0 = slot_or_null(fs[4], a.n_pleaf), z1 = slot_or_null(fs[5], a.n_pleaf);
+    if constexpr (ZD) {
+      const unsigned c0 = z0 * 512u + unsigned(h.c) + 7u, c1 = z1 * 512u + unsigned(h.c);
+      in.zf0 = ldv(a.flags + c0);
+      in.zf1 = ldv(a.flags + c1);
+      in.zr0 = ldv(r + c0);
+      in.zr1 = ldv(r + c1);
+      in.zq0 = ldv(pold + c0);
+      in.zq1 = ldv(pold + c1);
+    } else {
+      const T* zf = static_cast<const T*>(a.zf);
+      const unsigned zo0 = z0 * 384u + 64u + unsigned(h.fidx), zo1 = z1 * 384u + unsigned(h.fidx);
+      in.zf0 = ldv(a.zff + (z0 * 128u + 64u + unsigned(h.fidx)));
+      in.zf1 = ldv(a.zff + (z1 * 128u + unsigned(h.fidx)));
+      in.zr0 = ldv(zf + zo0);
+      in.zr1 = ldv(zf + zo1);
+      in.zq0 = ldv(zf + zo0 + 128 * qold);
+      in.zq1 = ldv(zf + zo1 + 128 * qold);
+    }
+    return;
+  }
+#endif
   const bool hv = hslot >= 0 && hslot < a.n_pleaf;
   const unsigned hb = unsigned(hv ? hslot : 0) * 512u + unsigned(hvox);
   in.hf = make_uint2(0u, 0u);
@@ -1479,6 +1537,21 @@ __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane
   const HalfLeaf h = half_pos(hw, lane);
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
+#if FSIM_PCG_NULLSLOT
+  if constexpr (std::is_same<T, float>::value) {
+    ldcol(p, slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox), in.H);
+    const unsigned z0 = slot_or_null(fs[4], a.n_pleaf), z1 = slot_or_null(fs[5], a.n_pleaf);
+    if constexpr (ZD) {
+      in.zm = ldv(p + (z0 * 512u + unsigned(h.c) + 7u));
+      in.zp = ldv(p + (z1 * 512u + unsigned(h.c)));
+    } else {
+      const T* zfp = static_cast<const T*>(a.zf) + (128u * unsigned(qcur) + unsigned(h.fidx));
+      in.zm = ldv(zfp + (z0 * 384u + 64u));
+      in.zp = ldv(zfp + z1 * 384u);
+    }
+    return;
+  }
+#endif
   if (hslot >= 0 && hslot < a.n_pleaf) {
     ldcol(p, unsigned(hslot) * 512u + unsigned(hvox), in.H);
   } else {
