@@ -63,7 +63,13 @@ UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50}
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
 # flushed before the launch) from one ncu capture of `bench.py --pcg-micro` on the 256^3
 # dam-break system (4.02 M unknowns); scaled by each step's unknowns.
-NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.94e6 / 4021250, "pcg_update": 61.35e6 / 4021250}
+NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.94e6 / 4021250, "pcg_update": 61.35e6 / 4021250,
+                           # the MIXED pair from a capture at 1024^3 (111,452,816 unknowns),
+                           # the size its solver is benchmarked at
+                           "pcg_spmv_mixed": 1.5765e9 / 111452816,
+                           "pcg_update_mixed": 2.3834e9 / 111452816}
+NCU_TRAFFIC_SOURCE = {"pcg_spmv": "256^3", "pcg_update": "256^3",
+                      "pcg_spmv_mixed": "1024^3", "pcg_update_mixed": "1024^3"}
 # The two launches of one PCG iteration (spmv then update) are reported as one unit: the
 # split of the iteration's work between them is a design choice (the update could take
 # x += alpha p or leave it), and their times are nearly equal.
@@ -394,7 +400,8 @@ def roofline(res):
             out["unfused_frac"] = achieved * ub / per / peak
         if all(k in NCU_TRAFFIC_PER_UNKNOWN for k in names):
             out["traffic"] = sum(NCU_TRAFFIC_PER_UNKNOWN[k] for k in names) * n_rows
-            out["traffic_source"] = "ncu capture of the 256^3 system (spmv + update), scaled by unknowns"
+            out["traffic_source"] = (f"ncu capture of the {NCU_TRAFFIC_SOURCE[names[0]]} system "
+                                     "(spmv + update), scaled by unknowns")
         pit = sum(res["piters"])
         prow = sum(r * it for r, it in zip(res["prows"], res["piters"]))
         out["per_kernel_profiled"] = {
@@ -406,7 +413,7 @@ def roofline(res):
                share_of_step=tot_ms / res["prof_ms"] if res["prof_ms"] > 0 else None)
     if name in NCU_TRAFFIC_PER_UNKNOWN and res["prows"]:
         out["traffic"] = NCU_TRAFFIC_PER_UNKNOWN[name] * float(np.mean(res["prows"]))
-        out["traffic_source"] = "ncu capture of the 256^3 system, scaled by unknowns"
+        out["traffic_source"] = f"ncu capture of the {NCU_TRAFFIC_SOURCE[name]} system, scaled by unknowns"
     if name in ALG_BYTES and res["prows"]:
         alg = ALG_BYTES[name] * float(np.mean(res["prows"]))
         tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["prows"], res["piters"]))

@@ -40,7 +40,9 @@ def test_mixed_pair_and_other_kernels():
     kt = {"pcg_spmv_mixed": (18.0, 750), "pcg_update_mixed": (17.0, 750)}
     r = bench.roofline(_res(kt, [30.0, 31.0]))
     assert "pcg_spmv_mixed + pcg_update_mixed" in r["kernel"]
-    assert r["traffic"] is None  # no ncu capture of the MIXED pair
+    per = bench.NCU_TRAFFIC_PER_UNKNOWN["pcg_spmv_mixed"] + bench.NCU_TRAFFIC_PER_UNKNOWN["pcg_update_mixed"]
+    assert r["traffic"] == pytest.approx(per * 4_050_000)
+    assert "1024^3" in r["traffic_source"]
     # a non-PCG top kernel is reported alone, from the profiled events
     kt = {"p2g_fused": (5.0, 3), "g2p": (1.0, 3)}
     r = bench.roofline(_res(kt, [0.0, 0.0]))
