@@ -61,8 +61,8 @@ ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update
 # (fp32 vectors), keyed by the spmv kernel of the pair.
 UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50}
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
-# flushed before the launch) from one ncu capture of `bench.py --pcg-micro` on the 256^3
-# dam-break system (4.02 M unknowns); scaled by each step's unknowns.
+# flushed before the launch) from ncu captures of `bench.py --pcg-micro`: the fp32 pair on
+# the 256^3 dam-break system (4.02 M unknowns); scaled by each step's unknowns.
 NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.94e6 / 4021250, "pcg_update": 61.35e6 / 4021250,
                            # the MIXED pair from a capture at 1024^3 (111,452,816 unknowns),
                            # the size its solver is benchmarked at
