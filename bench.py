@@ -727,8 +727,8 @@ def main():
         if rank != 0:
             return
         # One full reference FLIP step (the first step of the scene, PCG run
-        # to the workload's stopping rule) is the timed sample: about two
-        # minutes of single-thread CPU work at 256^3.
+        # to the workload's stopping rule) is the timed sample: about 50 s of
+        # single-thread CPU work at 256^3 on a Grace core, whatever --steps.
         t_step, npart, how = cpu_sample(args, None)
         v = 1.0 / t_step
         line = {"impl": "reference", "metric": "FLIP steps/s", "value": v, "unit": "steps/s",
