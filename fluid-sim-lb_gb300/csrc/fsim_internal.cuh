@@ -203,6 +203,7 @@ struct fsim_sim {
   // fsim_step: the rebinning gather moves pos and vel only; G2P rewrites
   // gvel for every live particle before anything reads it again
   bool gather_skip_gvel = false;
+  int pcg_last_iters = 0;         // iterations of the last graph-loop PCG segment
   float* io_early_pos = nullptr;  // host destination of the early position download
   int64_t io_early_cap = 0;
   int64_t io_early_n = -1;     // particles the early download copied (-1: none)

@@ -34,6 +34,7 @@
 // double-float sums per thread, fp64 above; plus an fp64 outer refinement
 // r = b - A x with x kept in fp64) and FP64 (fp64 vectors and dots).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <type_traits>
 
@@ -2096,18 +2097,32 @@ int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
   return FSIM_OK;
 }
 
-// Builds and launches graph = WHILE(cond){ (spmv; update) x kPassIters } on
-// the handle's stream: one pass runs kPassIters iterations of alternating
+// Builds and launches graph = WHILE(cond){ (spmv; update) x pass_iters } on
+// the handle's stream: one pass runs pass_iters iterations of alternating
 // parity (their buffers are fixed by PcgArgs::par), and kernels launched
 // after the stop flag is set return at once.  The head of the kernel that
 // sets the stop flag clears the condition.  Returns FSIM_OK, or
 // FSIM_ERR_CUDA when the graph API refuses (the caller then polls from the
 // host).  Kernel launches inside the graph are counted by the caller from
 // the iteration count the solve reports.
-constexpr int kPassIters = 8;  // PCG iterations per pass of the graph's WHILE body
+//
+// Pass length: each pass costs about 4 us of graph overhead, and the last
+// pass runs up to pass - 1 iterations of launches that return at once (about
+// 5 us each).  For I iterations the sum is smallest near pass = sqrt(1.7 I),
+// so the pass length follows the handle's previous solve: 8 iterations up to
+// about 150, 16 up to about 600, then 32 (even, so that a pass leaves the
+// launch parity where it found it).  FSIM_PCG_PASS_ITERS fixes it instead.
+#ifndef FSIM_PCG_PASS_ITERS
+#define FSIM_PCG_PASS_ITERS 0
+#endif
+int pass_iters_for(const fsim_sim* s) {
+  if (FSIM_PCG_PASS_ITERS > 0) return FSIM_PCG_PASS_ITERS;
+  const double p = std::sqrt(1.7 * double(s->pcg_last_iters));
+  return p >= 32.0 ? 32 : (p >= 16.0 ? 16 : 8);
+}
 
 template <typename T, int DM>
-int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl) {
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pass_iters) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -2127,7 +2142,7 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl) {
     ap[0].par = par0;
     ap[1].par = par0 ^ 1;
     cudaGraphNode_t prev = nullptr;
-    for (int k = 0; k < 2 * kPassIters && e == cudaSuccess; ++k) {
+    for (int k = 0; k < 2 * pass_iters && e == cudaSuccess; ++k) {
       cudaGraphNodeParams kn = {};
       kn.type = cudaGraphNodeTypeKernel;
       void* args[] = {&ap[(k >> 1) & 1]};
@@ -2243,21 +2258,23 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     // instruction, and their early-launched CTAs only hold SM slots (the
     // FP64 solve measured 20% slower with them).
     const bool pdl = s->use_pdl && std::is_same<T, float>::value && s->use_pipe && !s->use_tma;
+    const int pass_iters = pass_iters_for(s);
     if (pdl) {
-      rc = run_graph_loop<T, DM>(s, a, wgrid, par0, true);
+      rc = run_graph_loop<T, DM>(s, a, wgrid, par0, true, pass_iters);
       if (rc != FSIM_OK) s->use_pdl = false;  // programmatic edges refused: plain edges
     }
-    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, par0, false);
+    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, par0, false, pass_iters);
     if (rc == FSIM_OK) {
       lt.stop();
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
-      // each WHILE pass launches 2 * kPassIters kernels; the stop flag is
+      // each WHILE pass launches 2 * pass_iters kernels; the stop flag is
       // set in the head of iteration n (n = iterations completed here), so
-      // n / kPassIters + 1 passes ran
+      // n / pass_iters + 1 passes ran
       const int64_t n = std::max(s->h_sc->iter - it0, 0);
-      s->launches += 2 * kPassIters * (n / kPassIters + 1);
+      s->launches += 2 * pass_iters * (n / pass_iters + 1);
+      s->pcg_last_iters = int(std::min<int64_t>(n, 1 << 30));
       if (s->h_sc->bar_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG stage copy did not complete");
       return FSIM_OK;
     }
