@@ -251,18 +251,42 @@ __global__ void __launch_bounds__(256) k_p2g_nodes(const __grid_constant__ GridA
   int org[3];
   origin_of(a, s, org);
   float* vel = a.vel + int64_t(s) * 1536;
-  for (int v = tid; v < 512; v += 256) {
+  // this leaf's own block entries for both of the thread's nodes, loaded
+  // before either is used; the node loop then adds the neighbour particle
+  // leaves that cover a node with their outer layer (integer sums: the order
+  // does not matter)
+  unsigned long long own_v[2][3], own_w[2][3];
+  bool own_on[2];
+  {
+    const int ns = nb[nb_index(0, 0, 0)];
+    const bool own = ns >= 0 && ns < a.n_pleaf;
+    const unsigned long long* blk = a.p2g_nodes + int64_t(own ? ns : 0) * 6 * kNodeBlock;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int v = tid + 256 * j;
+      const int o = node_index(v >> 6, (v >> 3) & 7, v & 7);
+#pragma unroll
+      for (int D = 0; D < 3; ++D) {
+        own_v[j][D] = own ? blk[D * kNodeBlock + o] : 0ull;
+        own_w[j][D] = own ? blk[(3 + D) * kNodeBlock + o] : 0ull;
+      }
+      own_on[j] = own && ((a.p2g_touch[int64_t(ns) * 32 + (o >> 5)] >> (o & 31)) & 1u);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int v = tid + 256 * j;
     const int x = v >> 6, y = (v >> 3) & 7, z = v & 7;
     const int g[3] = {org[0] + x, org[1] + y, org[2] + z};
-    // this leaf's own block, then the neighbour particle leaves that cover
-    // the node with their outer layer
-    unsigned long long sv[3] = {0ull, 0ull, 0ull}, sw[3] = {0ull, 0ull, 0ull};
-    bool on = false;
+    unsigned long long sv[3] = {own_v[j][0], own_v[j][1], own_v[j][2]};
+    unsigned long long sw[3] = {own_w[j][0], own_w[j][1], own_w[j][2]};
+    bool on = own_on[j];
     const int dlo[3] = {x == 0 ? -1 : 0, y == 0 ? -1 : 0, z == 0 ? -1 : 0};
     const int dhi[3] = {x == 7 ? 1 : 0, y == 7 ? 1 : 0, z == 7 ? 1 : 0};
     for (int dx = dlo[0]; dx <= dhi[0]; ++dx)
       for (int dy = dlo[1]; dy <= dhi[1]; ++dy)
         for (int dz = dlo[2]; dz <= dhi[2]; ++dz) {
+          if (dx == 0 && dy == 0 && dz == 0) continue;  // the own block, loaded above
           const int ns = nb[nb_index(dx, dy, dz)];
           if (ns < 0 || ns >= a.n_pleaf) continue;
           const int o = node_index(x - 8 * dx, y - 8 * dy, z - 8 * dz);
