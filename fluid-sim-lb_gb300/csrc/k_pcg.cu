@@ -2321,6 +2321,9 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
   if (!prm) return fail(s, FSIM_ERR_INVALID, "pcg params missing");
   if (prm->mode < 0 || prm->mode > 2 || prm->precision < 0 || prm->precision > 2)
     return fail(s, FSIM_ERR_INVALID, "bad pcg mode/precision");
+  // the vectors hold the particle leaves and the zeroed null slot past them
+  if (int64_t(s->cap_pleaf) < int64_t(s->n_pleaf) + 1)
+    return fail(s, FSIM_ERR_STATE, "PCG vectors not sized for the leaf topology");
   int rc = ensure_pcg_vectors(s, prm->precision);
   if (rc) return rc;
   s->pcg_loop_ms = 0.0;
