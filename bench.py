@@ -25,9 +25,11 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -92,11 +94,12 @@ class Clocks:
     def __init__(self, dev: int):
         self.dev = dev
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        fd, name = tempfile.mkstemp(prefix="fsim_clocks_", suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -118,6 +121,15 @@ class Clocks:
             self.fh.close()
 
     def summary(self):
+        try:
+            return self._summary()
+        finally:
+            try:
+                self.path.unlink()
+            except OSError:
+                pass
+
+    def _summary(self):
         if self.proc is None or not self.path.exists():
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, mx, reasons = [], [], set()
@@ -425,82 +437,76 @@ def roofline(res):
     return out
 
 
-def cpu_sample(args, iters_per_step=None):
-    """The oracle on a bounded sample of the same workload (single thread).
+def host_cpu():
+    """(threads, CPU model) of the host the CPU legs run on."""
+    model = platform.processor() or platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return os.cpu_count() or 1, model
 
-    Times the first step of the scene stage by stage.  With iters_per_step
-    given, the PCG runs only args.cpu_pcg_iters iterations: its setup and
-    per-iteration cost are measured and the step time is extrapolated to
-    iters_per_step iterations (the GPU's mean for its timed steps).  Without
-    it the PCG runs to the workload's own stopping rule.
-    """
+
+def oracle_steps(args, warmup, steps):
+    """The oracle (the CPU restatement of the reference's single-partition
+    FLIP path) on the workload: `warmup` untimed steps, then `steps` timed
+    steps, each one full RunOneStep plus the CFL that sizes the next dt, with
+    the dt rule of the GPU arm.  Every host thread works on the loops whose
+    results do not depend on the thread count (the oracle is bit-identical
+    for any thread count); the P2G write-back stays serial.  Returns
+    (per-step seconds, per-step PCG iterations, particles, unknowns, threads)."""
     import fsim
-    from oracle.oracle import OracleSim
+    from oracle import oracle as O
 
+    threads, _ = host_cpu()
+    O.set_threads(threads)
     wl = WORKLOADS[args.workload]
     n = wl["n"]
     g, f = fsim.physical_gravity(n)
-    orc = OracleSim((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8)
+    orc = O.OracleSim((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8)
     orc.seed(fsim.scene_passes(wl["scene"], n), seed=0)
     npart = orc.particle_count()
-    dt, _ = fsim_dt(orc.cfl(), 0.0)
-    clock = time.perf_counter
-    t0 = clock()
-    orc.move_particles(dt)
-    orc.clear_grid()
-    orc.transfer_particles_to_grid()
-    orc.apply_boundary_conditions()
-    orc.save_grid_velocities()
-    orc.delete_outside_particles()
-    orc.reinitialize_phi()
-    orc.add_gravity(dt)
-    orc.apply_boundary_conditions()
-    orc.compute_divergence()
-    t_pre = clock() - t0
-    if iters_per_step is None:
-        t0 = clock()
-        st = orc.pcg_solve(mode=1, precision=0, max_iterations=args.max_iterations, tol=args.tol)
-        t_pcg = clock() - t0
-        iters = st.iterations
-        how = f"{iters} PCG iterations run in full"
-    else:
-        m = args.cpu_pcg_iters
-        t0 = clock()
-        orc.pcg_solve(mode=2, precision=0, max_iterations=0)
-        t_setup = clock() - t0
-        t0 = clock()
-        orc.pcg_solve(mode=2, precision=0, max_iterations=m)
-        t_m = clock() - t0
-        per_it = max(t_m - t_setup, 0.0) / m
-        iters = iters_per_step
-        t_pcg = t_setup + per_it * iters
-        how = (f"PCG setup + {m} iterations timed ({per_it * 1e3:.1f} ms/iteration), "
-               f"extrapolated to {iters:.1f} iterations/step")
-    t0 = clock()
-    orc.update_velocity_from_pressure()
-    orc.get_velocity_update()
-    orc.update_particles_from_grid()
-    t_post = clock() - t0
-    t_step = t_pre + t_pcg + t_post
-    return t_step, npart, how
+    inv, t_in = orc.cfl(), 0.0
+    for _ in range(warmup):
+        dt, t_in = fsim_dt(inv, t_in)
+        orc.step(dt, mode=1, precision=0, max_iterations=args.max_iterations, tol=args.tol)
+        inv = orc.cfl()
+    secs, iters, rows = [], [], []
+    for _ in range(steps):
+        dt, t_in = fsim_dt(inv, t_in)
+        t0 = time.perf_counter()
+        st = orc.step(dt, mode=1, precision=0, max_iterations=args.max_iterations, tol=args.tol)
+        inv = orc.cfl()
+        secs.append(time.perf_counter() - t0)
+        iters.append(st.iterations)
+        rows.append(st.n_rows)
+    orc.close()
+    O.set_threads(1)
+    return secs, iters, npart, (float(np.mean(rows)) if rows else None), threads
 
 
-def pcg_compare(args):
-    """Mixed-precision vs FP32 PCG on one divergence (the 512^3 multi-dam).
+def pcg_compare(args, workload):
+    """Mixed-precision vs FP32 PCG on one divergence (default: the 512^3
+    multi-dam of the mixed-precision configuration).
 
     Runs one step to build the system, then solves it again with: an FP64
     PCG to relative residual 1e-12 (the reference solution x64; the GPU FP64
     path is checked against the FP64 oracle solve in tests/test_gpu_pcg.py),
-    plain FP32 PCG and MIXED PCG (FP32 inner iterations with FP64-accumulated
-    dots, FP64 outer residual refinement) at a ladder of tolerances.  Each
-    solve is timed with CUDA events on the library's stream; its error is
-    ||x - x64|| / ||x64|| over the fluid cells.  Prints one JSON line.
+    plain FP32 PCG, MIXED PCG (fp32 vectors; dot products accumulated as
+    double-float pairs, about 44 significant bits, not FP64; fp64 outer
+    residual replacement) and FP64 PCG at ladders of tolerances.  Each solve
+    is timed with CUDA events on the library's stream; its error is
+    ||x - x64|| / ||x64|| over the fluid cells.  Returns the record.
     """
     import torch
 
     import fsim
 
-    wl = WORKLOADS[args.workload]
+    wl = WORKLOADS[workload]
     sim = make_sim(wl, args, 0)
     stream = torch.cuda.ExternalStream(sim.stream(), device=0)
     st = sim.step(0.01, fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 3000, tolerance=1e-5))
@@ -520,7 +526,9 @@ def pcg_compare(args):
                                                 tolerance=1e-12))
     nref = np.linalg.norm(xref)
     out = {"metric": "PCG time to relative error vs FP64 solution", "unit": "ms",
-           "workload": args.workload, "unknowns": rows,
+           "workload": workload, "unknowns": rows,
+           "mixed_dots": "double-float pairs (about 44 significant bits), not FP64; "
+                         "alpha and beta formed in FP64",
            "fp64_reference": {"ms": t_ref, "iterations": st_ref.iterations,
                               "rel_residual": float(np.sqrt(st_ref.rr / st_ref.bb))},
            "fp32": [], "mixed": [], "fp64": []}
@@ -554,8 +562,11 @@ def pcg_compare(args):
     out["fastest_fp64_at_1e-6"] = bd
     out["speedup_mixed_vs_fp32"] = (bf["ms"] / bm["ms"]) if (bf and bm) else None
     out["speedup_mixed_vs_fp64"] = (bd["ms"] / bm["ms"]) if (bd and bm) else None
-    print(json.dumps(out), flush=True)
+    # the dots' precision does not limit MIXED: it needs FP64's iteration count
+    if bm and bd:
+        out["iterations_mixed_vs_fp64_at_1e-6"] = [bm["iterations"], bd["iterations"]]
     sim.close()
+    return out
 
 
 def pcg_micro(args):
@@ -687,6 +698,8 @@ def main():
     ap.add_argument("--cpu-pcg-iters", type=int, default=40)
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-pcg-compare", action="store_true",
+                    help="leave the 512^3 mixed-vs-FP32-vs-FP64 PCG record out of the bench line")
     ap.add_argument("--pcg-compare", action="store_true",
                     help="mixed vs FP32 PCG time to 1e-6 error (use --workload multidam_512)")
     ap.add_argument("--pcg-micro", action="store_true",
@@ -714,7 +727,7 @@ def main():
               "parallelism": f"replicas x{world}"}
 
     if args.pcg_compare:
-        pcg_compare(args)
+        print(json.dumps(pcg_compare(args, args.workload)), flush=True)
         return
     if args.pcg_micro:
         pcg_micro(args)
@@ -726,19 +739,29 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # One full reference FLIP step (the first step of the scene, PCG run
-        # to the workload's stopping rule) is the timed sample: about 50 s of
-        # single-thread CPU work at 256^3 on a Grace core, whatever --steps.
-        t_step, npart, how = cpu_sample(args, None)
-        v = 1.0 / t_step
+        # The same steps as the GPU arm: W untimed warm-up steps, then K timed
+        # steps of the oracle, each a full RunOneStep (no extrapolation).
+        secs, iters, npart, rows, threads = oracle_steps(args, args.warmup, args.steps)
+        _, model = host_cpu()
+        total = sum(secs)
+        v = args.steps / total
         line = {"impl": "reference", "metric": "FLIP steps/s", "value": v, "unit": "steps/s",
-                "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * t_step,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": config,
-                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
-                                 "sample": f"first step of {args.workload} ({npart} particles; "
-                                           f"{how}); oracle restatement of the reference CPU "
-                                           f"path, one thread (one partition, TBB at 1 thread)"},
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config,
+                "workload_stats": {"particles": npart, "fluid_cells": rows,
+                                   "pcg_iters_per_step": float(np.mean(iters)),
+                                   "pcg_iters": iters},
+                "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                                 "host": model,
+                                 "sample": f"steps {args.warmup + 1}-{args.warmup + args.steps} "
+                                           f"of {args.workload} ({npart} particles) after "
+                                           f"{args.warmup} untimed warm-up steps, each a full "
+                                           f"step; the oracle's restatement of the reference "
+                                           f"CPU path on {threads} host threads (its loops "
+                                           f"with thread-count-independent results; the "
+                                           f"P2G write-back stays on one)"},
                 "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -755,9 +778,10 @@ def main():
     line = {"metric": "FLIP steps/s", "value": value, "unit": "steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": dict(config, particles=res["n_particles"],
-                                                 fluid_cells=res["n_fluid"],
-                                                 pcg_iters_per_step=float(np.mean(res["iters"]))),
+            "data": "synthetic", "config": config,
+            "workload_stats": {"particles": res["n_particles"], "fluid_cells": res["n_fluid"],
+                               "pcg_iters_per_step": float(np.mean(res["iters"])),
+                               "pcg_iters": res["iters"]},
             "roofline": roofline(res),
             "e2e": {"value": whole_job_rate(world, 1, res["e2e_ms"]), "unit": "steps/s",
                     "h2d_bytes_per_step": res["e2e_bytes"], "d2h_bytes_per_step": res["e2e_bytes"],
@@ -766,12 +790,18 @@ def main():
             "device_memory_gb": round(res["device_memory_gb"], 2),
             "kernels_ms": {k: round(v[0], 3) for k, v in sorted(res["kt"].items(),
                                                                 key=lambda kv: -kv[1][0])}}
+    if not args.no_pcg_compare:
+        line["pcg_compare"] = pcg_compare(args, "multidam_512")
     if not args.no_cpu:
-        t_step, npart, how = cpu_sample(args, float(np.mean(res["iters"])))
-        line["cpu_baseline"] = {"value": 1.0 / t_step, "unit": "steps/s", "cores": 1,
-                                "kind": "port",
-                                "sample": f"first step of {args.workload} ({npart} particles), "
-                                          f"stages timed on one thread; {how}"}
+        secs, iters, npart, _, threads = oracle_steps(args, 0, 1)
+        _, model = host_cpu()
+        line["cpu_baseline"] = {"value": 1.0 / secs[0], "unit": "steps/s", "cores": threads,
+                                "kind": "port", "host": model,
+                                "sample": f"first step of {args.workload} ({npart} particles, "
+                                          f"{iters[0]} PCG iterations), one full step of the "
+                                          f"oracle on {threads} host threads; the reference arm "
+                                          f"(--impl reference) times the same steps as this "
+                                          f"line"}
     print(json.dumps(line), flush=True)
 
 

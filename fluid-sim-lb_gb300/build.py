@@ -80,7 +80,7 @@ def build_oracle(force: bool = False) -> Path:
     so = out_dir / "liboracle_fsim.so"
     src = ORACLE / "oracle.cc"
     if force or _stale(so, [src, ORACLE / "oracle.h"]):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
               "-fno-fast-math", "-Wall", "-o", str(so), str(src)])
     return so
 

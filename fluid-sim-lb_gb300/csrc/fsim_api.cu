@@ -250,10 +250,6 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   // FSIM_PCG_PDL=0: plain edges between the graph's kernel nodes (default:
   // programmatic edges, each kernel launching while its predecessor finishes)
   if (const char* c = std::getenv("FSIM_PCG_PDL")) s->use_pdl = c[0] != '0';
-  // FSIM_PCG_COOP=1: the PCG iterations as one persistent cooperative kernel
-  if (const char* c = std::getenv("FSIM_PCG_COOP")) s->use_coop = c[0] == '1';
-  // FSIM_PCG_TMA=1: the spmv with bulk-copy staged own columns (FP32 dots)
-  if (const char* c = std::getenv("FSIM_PCG_TMA")) s->use_tma = c[0] == '1';
   // FSIM_PCG_ZDIRECT=0/1: z-face planes or direct reads (default: by system size)
   if (const char* c = std::getenv("FSIM_PCG_ZDIRECT")) s->zdirect = c[0] == '1' ? 1 : 0;
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels

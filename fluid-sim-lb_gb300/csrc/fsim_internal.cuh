@@ -159,9 +159,6 @@ struct alignas(16) PcgScalars {
   double tol2_outer;  // MIXED: outer tolerance squared; a segment never stops below tol2_outer*bb
   unsigned int cnt_s, cnt_r;
   unsigned long long n_rows;  // FLUID cells (unknowns), counted by setup
-  // grid barrier of the persistent (cooperative) PCG loop
-  unsigned int bar_count, bar_gen, bar_err, bar_pad;
-  double bar_tot[2];  // totals the barrier's last block publishes
   // hot-loop hand-off: [0] spmv -> update, [1] update -> spmv (and setup /
   // residual replacement -> spmv)
   PcgIterState st[2];
@@ -203,7 +200,11 @@ struct fsim_sim {
   // fsim_step: the rebinning gather moves pos and vel only; G2P rewrites
   // gvel for every live particle before anything reads it again
   bool gather_skip_gvel = false;
-  int pcg_last_iters = 0;         // iterations of the last graph-loop PCG segment
+  // graph-loop pass length: the longest graph-loop segment of the previous
+  // solve (a MIXED solve runs several; its last one is often short), and the
+  // longest of the solve in progress
+  int pcg_last_iters = 0;
+  int pcg_seg_max = 0;
   float* io_early_pos = nullptr;  // host destination of the early position download
   int64_t io_early_cap = 0;
   int64_t io_early_n = -1;     // particles the early download copied (-1: none)
@@ -289,12 +290,6 @@ struct fsim_sim {
   bool use_graphs = true;
   // its kernel nodes joined by programmatic (early-launch) edges
   bool use_pdl = true;
-  // PCG iterations as one cooperative persistent kernel with grid barriers
-  // (measured slower than the graph loop at 256^3: 42.5 vs 38.9 us per
-  // iteration; opt-in)
-  bool use_coop = false;
-  // spmv with the own columns staged by bulk copies (FSIM_PCG_TMA=1)
-  bool use_tma = false;
   // z-face neighbours of the pipelined kernels: -1 by system size, 0 planes,
   // 1 direct reads (FSIM_PCG_ZDIRECT)
   int zdirect = -1;

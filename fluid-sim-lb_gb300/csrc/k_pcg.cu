@@ -40,12 +40,6 @@
 
 #include "fsim_internal.cuh"
 
-// Halo and z-face loads of missing neighbours read a zeroed null slot (see
-// slot_or_null); 0 restores the validity branches.
-#ifndef FSIM_PCG_NULLSLOT
-#define FSIM_PCG_NULLSLOT 1
-#endif
-
 namespace fsim {
 
 namespace {
@@ -328,7 +322,6 @@ template <typename T, int DM>
 __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ PcgArgs a) {
   T* x = static_cast<T*>(a.x);
   T* r = static_cast<T*>(a.r);
-#if FSIM_PCG_NULLSLOT
   if (std::is_same<T, float>::value && blockIdx.x == gridDim.x - 1) {
     // the null slot n_pleaf read by the pipelined kernels' halo loads
     const int64_t o = int64_t(a.n_pleaf) * 512;
@@ -342,7 +335,6 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
       static_cast<T*>(a.zf)[int64_t(a.n_pleaf) * 384 + v] = T(0);
     for (int v = threadIdx.x; v < 128; v += kThreads) a.zff[int64_t(a.n_pleaf) * 128 + v] = 0;
   }
-#endif
   Dot<DM> drr, drz, dbb;
   int nfluid = 0;
   for (int s = blockIdx.x; s < a.n_pleaf; s += gridDim.x) {
@@ -434,27 +426,15 @@ struct Col {
   T v[8];
 };
 
-// Column loads of the 128-bit form (FSIM_PCG_COL256=0): a lane reads its 32 B
-// column as two 16 B vectors; FSIM_PCG_LDCG=1 makes them L2-only.
-#ifndef FSIM_PCG_LDCG
-#define FSIM_PCG_LDCG 0
-#endif
 template <typename V>
 __device__ __forceinline__ V ldv(const V* p) {
-#if FSIM_PCG_LDCG
-  return __ldcg(p);
-#else
   return *p;
-#endif
 }
 
 // Column offsets are multiples of 8 cells, so a float column starts 32-byte
 // aligned: it moves as one 256-bit access per lane (sm_100 and later).  Two
 // 128-bit accesses would each touch every 128-byte line of the half leaf, so
 // the L1 pipeline would see each line twice.
-#ifndef FSIM_PCG_COL256
-#define FSIM_PCG_COL256 1
-#endif
 __device__ __forceinline__ void unpack2(unsigned long long u, float& lo, float& hi) {
   lo = __uint_as_float(unsigned(u));
   hi = __uint_as_float(unsigned(u >> 32));
@@ -463,21 +443,13 @@ __device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
   return (static_cast<unsigned long long>(__float_as_uint(hi)) << 32) | __float_as_uint(lo);
 }
 __device__ __forceinline__ void ldcol(const float* __restrict__ p, int64_t o, Col<float>& c) {
-#if FSIM_PCG_COL256 && !FSIM_PCG_LDCG
   const ulonglong4_32a a = *reinterpret_cast<const ulonglong4_32a*>(p + o);
   unpack2(a.x, c.v[0], c.v[1]);
   unpack2(a.y, c.v[2], c.v[3]);
   unpack2(a.z, c.v[4], c.v[5]);
   unpack2(a.w, c.v[6], c.v[7]);
-#else
-  const float4 a = ldv(reinterpret_cast<const float4*>(p + o));
-  const float4 b = ldv(reinterpret_cast<const float4*>(p + o + 4));
-  c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
-  c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
-#endif
 }
 __device__ __forceinline__ void ldcol(const double* __restrict__ p, int64_t o, Col<double>& c) {
-#if FSIM_PCG_COL256 && !FSIM_PCG_LDCG
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const double4_32a a = *reinterpret_cast<const double4_32a*>(p + o + 4 * k);
@@ -486,30 +458,16 @@ __device__ __forceinline__ void ldcol(const double* __restrict__ p, int64_t o, C
     c.v[4 * k + 2] = a.z;
     c.v[4 * k + 3] = a.w;
   }
-#else
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const double2 a = ldv(reinterpret_cast<const double2*>(p + o + 2 * k));
-    c.v[2 * k] = a.x;
-    c.v[2 * k + 1] = a.y;
-  }
-#endif
 }
 __device__ __forceinline__ void stcol(float* __restrict__ p, int64_t o, const Col<float>& c) {
-#if FSIM_PCG_COL256
   ulonglong4_32a a;
   a.x = pack2(c.v[0], c.v[1]);
   a.y = pack2(c.v[2], c.v[3]);
   a.z = pack2(c.v[4], c.v[5]);
   a.w = pack2(c.v[6], c.v[7]);
   *reinterpret_cast<ulonglong4_32a*>(p + o) = a;
-#else
-  *reinterpret_cast<float4*>(p + o) = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
-  *reinterpret_cast<float4*>(p + o + 4) = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
-#endif
 }
 __device__ __forceinline__ void stcol(double* __restrict__ p, int64_t o, const Col<double>& c) {
-#if FSIM_PCG_COL256
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     double4_32a a;
@@ -518,26 +476,6 @@ __device__ __forceinline__ void stcol(double* __restrict__ p, int64_t o, const C
     a.z = c.v[4 * k + 2];
     a.w = c.v[4 * k + 3];
     *reinterpret_cast<double4_32a*>(p + o + 4 * k) = a;
-  }
-#else
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
-    *reinterpret_cast<double2*>(p + o + 2 * k) = make_double2(c.v[2 * k], c.v[2 * k + 1]);
-#endif
-}
-// L2-only column load (data another CTA wrote earlier in the same launch)
-__device__ __forceinline__ void ldcol_cg(const float* p, int64_t o, Col<float>& c) {
-  const float4 a = __ldcg(reinterpret_cast<const float4*>(p + o));
-  const float4 b = __ldcg(reinterpret_cast<const float4*>(p + o + 4));
-  c.v[0] = a.x; c.v[1] = a.y; c.v[2] = a.z; c.v[3] = a.w;
-  c.v[4] = b.x; c.v[5] = b.y; c.v[6] = b.z; c.v[7] = b.w;
-}
-__device__ __forceinline__ void ldcol_cg(const double* p, int64_t o, Col<double>& c) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const double2 a = __ldcg(reinterpret_cast<const double2*>(p + o + 2 * k));
-    c.v[2 * k] = a.x;
-    c.v[2 * k + 1] = a.y;
   }
 }
 __device__ __forceinline__ uint2 ldflags(const uint8_t* __restrict__ f, int64_t o) {
@@ -1157,7 +1095,7 @@ __device__ __forceinline__ void spmv_load_own(const PcgArgs& a, int hw, int lane
 // ZD: z-face neighbours read from the vectors (large systems) instead of the
 // published planes.
 //
-// FSIM_PCG_NULLSLOT: a missing neighbour (no leaf, or a leaf without PCG
+// A missing neighbour (no leaf, or a leaf without PCG
 // unknowns) reads slot n_pleaf instead, which the setup zeroes (flags, r,
 // both p and their z-face planes) and no kernel writes during the solve, so
 // the loads need no validity branch.  The particle-leaf capacity keeps that
@@ -1172,69 +1110,30 @@ __device__ __forceinline__ void spmv_load_halo(const PcgArgs& a, int hw, int lan
   const HalfLeaf h = half_pos(hw, lane);
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
-#if FSIM_PCG_NULLSLOT
-  if constexpr (std::is_same<T, float>::value) {
-    const unsigned hb = slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox);
-    in.hf = ldflags(a.flags, hb);
-    ldcol(r, hb, in.hr);
-    ldcol(pold, hb, in.hp);
-    const unsigned z0 = slot_or_null(fs[4], a.n_pleaf), z1 = slot_or_null(fs[5], a.n_pleaf);
-    if constexpr (ZD) {
-      const unsigned c0 = z0 * 512u + unsigned(h.c) + 7u, c1 = z1 * 512u + unsigned(h.c);
-      in.zf0 = ldv(a.flags + c0);
-      in.zf1 = ldv(a.flags + c1);
-      in.zr0 = ldv(r + c0);
-      in.zr1 = ldv(r + c1);
-      in.zq0 = ldv(pold + c0);
-      in.zq1 = ldv(pold + c1);
-    } else {
-      const T* zf = static_cast<const T*>(a.zf);
-      const unsigned zo0 = z0 * 384u + 64u + unsigned(h.fidx), zo1 = z1 * 384u + unsigned(h.fidx);
-      in.zf0 = ldv(a.zff + (z0 * 128u + 64u + unsigned(h.fidx)));
-      in.zf1 = ldv(a.zff + (z1 * 128u + unsigned(h.fidx)));
-      in.zr0 = ldv(zf + zo0);
-      in.zr1 = ldv(zf + zo1);
-      in.zq0 = ldv(zf + zo0 + 128 * qold);
-      in.zq1 = ldv(zf + zo1 + 128 * qold);
-    }
-    return;
-  }
-#endif
-  const bool hv = hslot >= 0 && hslot < a.n_pleaf;
-  const unsigned hb = unsigned(hv ? hslot : 0) * 512u + unsigned(hvox);
-  in.hf = make_uint2(0u, 0u);
-  if (hv) {
-    in.hf = ldflags(a.flags, hb);
-    ldcol(r, hb, in.hr);
-    ldcol(pold, hb, in.hp);
-  } else {
-#pragma unroll
-    for (int z = 0; z < 8; ++z) in.hr.v[z] = in.hp.v[z] = T(0);
-  }
-  const int zs0 = fs[4], zs1 = fs[5];
-  const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+  static_assert(std::is_same<T, float>::value, "the pipelined kernels take fp32 vectors");
+  const unsigned hb = slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox);
+  in.hf = ldflags(a.flags, hb);
+  ldcol(r, hb, in.hr);
+  ldcol(pold, hb, in.hp);
+  const unsigned z0 = slot_or_null(fs[4], a.n_pleaf), z1 = slot_or_null(fs[5], a.n_pleaf);
   if constexpr (ZD) {
-    // the -z neighbour's cell (x, y, 7) and the +z neighbour's (x, y, 0): their
-    // leaves are processed at about the same time, so the loads hit L2
-    const unsigned c0 = unsigned(zv0 ? zs0 : 0) * 512u + unsigned(h.c) + 7u;
-    const unsigned c1 = unsigned(zv1 ? zs1 : 0) * 512u + unsigned(h.c);
-    in.zf0 = zv0 ? ldv(a.flags + c0) : uint8_t(0);
-    in.zf1 = zv1 ? ldv(a.flags + c1) : uint8_t(0);
-    in.zr0 = zv0 ? ldv(r + c0) : T(0);
-    in.zr1 = zv1 ? ldv(r + c1) : T(0);
-    in.zq0 = zv0 ? ldv(pold + c0) : T(0);
-    in.zq1 = zv1 ? ldv(pold + c1) : T(0);
-    return;
+    const unsigned c0 = z0 * 512u + unsigned(h.c) + 7u, c1 = z1 * 512u + unsigned(h.c);
+    in.zf0 = ldv(a.flags + c0);
+    in.zf1 = ldv(a.flags + c1);
+    in.zr0 = ldv(r + c0);
+    in.zr1 = ldv(r + c1);
+    in.zq0 = ldv(pold + c0);
+    in.zq1 = ldv(pold + c1);
+  } else {
+    const T* zf = static_cast<const T*>(a.zf);
+    const unsigned zo0 = z0 * 384u + 64u + unsigned(h.fidx), zo1 = z1 * 384u + unsigned(h.fidx);
+    in.zf0 = ldv(a.zff + (z0 * 128u + 64u + unsigned(h.fidx)));
+    in.zf1 = ldv(a.zff + (z1 * 128u + unsigned(h.fidx)));
+    in.zr0 = ldv(zf + zo0);
+    in.zr1 = ldv(zf + zo1);
+    in.zq0 = ldv(zf + zo0 + 128 * qold);
+    in.zq1 = ldv(zf + zo1 + 128 * qold);
   }
-  const T* zf = static_cast<const T*>(a.zf);
-  const unsigned zo0 = unsigned(zv0 ? zs0 : 0) * 384u + 64u + unsigned(h.fidx);
-  const unsigned zo1 = unsigned(zv1 ? zs1 : 0) * 384u + unsigned(h.fidx);
-  in.zf0 = zv0 ? ldv(a.zff + (unsigned(zs0) * 128u + 64u + unsigned(h.fidx))) : uint8_t(0);
-  in.zf1 = zv1 ? ldv(a.zff + (unsigned(zs1) * 128u + unsigned(h.fidx))) : uint8_t(0);
-  in.zr0 = zv0 ? ldv(zf + zo0) : T(0);
-  in.zr1 = zv1 ? ldv(zf + zo1) : T(0);
-  in.zq0 = zv0 ? ldv(zf + zo0 + 128 * qold) : T(0);
-  in.zq1 = zv1 ? ldv(zf + zo1 + 128 * qold) : T(0);
 }
 
 template <typename T, bool ZD>
@@ -1326,194 +1225,6 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   put_partials<DM, 1>(a, kPartPAp, v);
 }
 
-// ---- bulk-copy (TMA) staging of the own columns ---------------------------------
-// A half leaf's own r, p_{j-1} and flags are 1 KB + 1 KB + 256 B, contiguous.
-// Lane 0 of each warp copies them into a ring of kStages shared-memory stages
-// with cp.async.bulk (the copy engine of the SM, no registers and no
-// load/store-unit slots), kStages - 1 half leaves ahead; an mbarrier per stage
-// counts the bytes in.  The halo column and the z faces (scattered, 32 B and
-// 4 B per lane) are still loaded into registers one half leaf ahead.
-constexpr int kStages = 3;
-constexpr unsigned kMbarPolls = 1u << 22;  // bounded wait on a stage
-
-struct SpmvStage {
-  float r[256];
-  float p[256];
-  uint8_t f[256];
-};
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) {
-  return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
-      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait; false if the stage did not fill within kMbarPolls polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-  for (unsigned i = 0; i < kMbarPolls; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-__device__ __forceinline__ void fence_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-}
-
-// Lane 0: copy half leaf hw's own columns into stage st.
-__device__ __forceinline__ void spmv_stage_issue(const PcgArgs& a, int hw, const float* r,
-                                                 const float* pold, SpmvStage& st,
-                                                 uint64_t* bar) {
-  const int64_t o = int64_t(hw >> 1) * 512 + (hw & 1) * 256;
-  mbar_expect_tx(bar, 2u * 1024u + 256u);
-  bulk_g2s(st.r, r + o, 1024u, bar);
-  bulk_g2s(st.p, pold + o, 1024u, bar);
-  bulk_g2s(st.f, a.flags + o, 256u, bar);
-}
-
-// k_pcg_spmv_pl with the own columns staged by bulk copies (fp32).
-template <int DM>
-__global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_constant__ PcgArgs a) {
-  pdl_wait();  // reads its predecessor's outputs from the start
-  pdl_trigger();
-  using T = float;
-  __shared__ Tile<T> tiles[kHotThreads / 32];
-  __shared__ DiagInv<T> tab[16];
-  __shared__ HeadStage<2, PartT<DM>> hs;
-  __shared__ __align__(128) SpmvStage stage[kHotThreads / 32][kStages];
-  __shared__ __align__(8) uint64_t bars[kHotThreads / 32][kStages];
-  const int par = a.par;
-  const T* r = static_cast<const T*>(a.r);
-  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
-  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
-  const int qold = 1 + (par ^ 1), qnew = 1 + par;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int wpb = kHotThreads / 32;
-  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
-  const int hw0 = blockIdx.x * wpb + w;
-  SpmvStage* stg = stage[w];
-  uint64_t* bar = bars[w];
-  if (lane == 0) {
-#pragma unroll
-    for (int q = 0; q < kStages; ++q) mbar_init(&bar[q], 1u);
-    fence_async_smem();
-  }
-  __syncwarp();
-  if (lane == 0) {
-    for (int q = 0; q < kStages - 1; ++q) {
-      const int hq = hw0 + q * hstride;
-      if (hq < nhw) spmv_stage_issue(a, hq, r, pold, stg[q], &bar[q]);
-    }
-  }
-  head_issue<DM, 2>(hs, a, 0);
-  fill_diag_table<T>(tab);
-  SpmvIn<T> cur;  // halo and z faces only (rc, pc, f come from the stage)
-  int nbl = -1;
-  if (hw0 < nhw) {
-    int fs[6];
-    face_slots(face_slot_lane(a.nbr, hw0 >> 1, lane), fs);
-    nbl = hw0 + hstride < nhw ? face_slot_lane(a.nbr, (hw0 + hstride) >> 1, lane) : -1;
-    spmv_load_halo<T, false>(a, hw0, lane, fs, r, pold, qold, cur);
-  }
-  const HotHead head = spmv_head<DM>(hs, a);
-  bool ok = true;
-  if (head.done) {
-    // no work: drain the copies already issued before leaving
-    for (int q = 0; q < kStages - 1; ++q)
-      if (hw0 + q * hstride < nhw) mbar_wait(&bar[q], 0u);
-    return;
-  }
-  const T beta = T(head.s);
-  Tile<T>& tile = tiles[w];
-  Dot<DM> dp;
-  int k = 0;
-  for (int hw = hw0; hw < nhw; hw += hstride, ++k) {
-    // keep kStages - 1 half leaves in flight: refill the stage read last time
-    {
-      const int hq = hw + (kStages - 1) * hstride;
-      const int q = (k + kStages - 1) % kStages;
-      if (lane == 0 && hq < nhw) spmv_stage_issue(a, hq, r, pold, stg[q], &bar[q]);
-    }
-    const int hn = hw + hstride;
-    SpmvIn<T> nxt;
-    if (hn < nhw) {
-      int fs[6];
-      face_slots(nbl, fs);
-      spmv_load_halo<T, false>(a, hn, lane, fs, r, pold, qold, nxt);
-      nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
-    }
-    const int q = k % kStages;
-    if (!mbar_wait(&bar[q], unsigned((k / kStages) & 1))) ok = false;
-    const HalfLeaf h = half_pos(hw, lane);
-    {
-      const float4 a0 = reinterpret_cast<const float4*>(stg[q].r)[2 * lane];
-      const float4 a1 = reinterpret_cast<const float4*>(stg[q].r)[2 * lane + 1];
-      const float4 b0 = reinterpret_cast<const float4*>(stg[q].p)[2 * lane];
-      const float4 b1 = reinterpret_cast<const float4*>(stg[q].p)[2 * lane + 1];
-      cur.f = reinterpret_cast<const uint2*>(stg[q].f)[lane];
-      cur.rc.v[0] = a0.x; cur.rc.v[1] = a0.y; cur.rc.v[2] = a0.z; cur.rc.v[3] = a0.w;
-      cur.rc.v[4] = a1.x; cur.rc.v[5] = a1.y; cur.rc.v[6] = a1.z; cur.rc.v[7] = a1.w;
-      cur.pc.v[0] = b0.x; cur.pc.v[1] = b0.y; cur.pc.v[2] = b0.z; cur.pc.v[3] = b0.w;
-      cur.pc.v[4] = b1.x; cur.pc.v[5] = b1.y; cur.pc.v[6] = b1.z; cur.pc.v[7] = b1.w;
-    }
-    __syncwarp();
-    if (lane == 0) fence_async_smem();  // this stage's reads before its next bulk write
-    Col<T> P, H;
-#pragma unroll
-    for (int z = 0; z < 8; ++z) {
-      P.v[z] = pnew_of<T>(tab, fbyte(cur.f, z), cur.rc.v[z], cur.pc.v[z], beta);
-      H.v[z] = pnew_of<T>(tab, fbyte(cur.hf, z), cur.hr.v[z], cur.hp.v[z], beta);
-    }
-    const T zm = pnew_of<T>(tab, cur.zf0, cur.zr0, cur.zq0, beta);
-    const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
-    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
-    stcol(pnew, o, P);
-    {  // publish the z faces for the neighbours
-      T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
-      zw[0] = P.v[0];
-      zw[64] = P.v[7];
-    }
-    __syncwarp();
-    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
-    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
-    __syncwarp();
-    Col<T> ap;
-    stencil_col<T>(tile, tab, h.lx, h.cy, P, cur.f, zm, zp, ap);
-#pragma unroll
-    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
-    cur.hf = nxt.hf;
-    cur.hr = nxt.hr;
-    cur.hp = nxt.hp;
-    cur.zf0 = nxt.zf0; cur.zf1 = nxt.zf1;
-    cur.zr0 = nxt.zr0; cur.zr1 = nxt.zr1;
-    cur.zq0 = nxt.zq0; cur.zq1 = nxt.zq1;
-  }
-  if (!ok && lane == 0) atomicExch(&a.sc->bar_err, 2u);  // a stage never filled
-  PartT<DM> v[1] = {dp.pvalue()};
-  put_partials<DM, 1>(a, kPartPAp, v);
-}
-
 template <typename T>
 struct UpdIn {
   uint2 f;
@@ -1538,37 +1249,17 @@ __device__ __forceinline__ void upd_load_halo(const PcgArgs& a, int hw, int lane
   const HalfLeaf h = half_pos(hw, lane);
   int hslot, hvox;
   halo_col(h, fs, hslot, hvox);
-#if FSIM_PCG_NULLSLOT
-  if constexpr (std::is_same<T, float>::value) {
-    ldcol(p, slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox), in.H);
-    const unsigned z0 = slot_or_null(fs[4], a.n_pleaf), z1 = slot_or_null(fs[5], a.n_pleaf);
-    if constexpr (ZD) {
-      in.zm = ldv(p + (z0 * 512u + unsigned(h.c) + 7u));
-      in.zp = ldv(p + (z1 * 512u + unsigned(h.c)));
-    } else {
-      const T* zfp = static_cast<const T*>(a.zf) + (128u * unsigned(qcur) + unsigned(h.fidx));
-      in.zm = ldv(zfp + (z0 * 384u + 64u));
-      in.zp = ldv(zfp + z1 * 384u);
-    }
-    return;
-  }
-#endif
-  if (hslot >= 0 && hslot < a.n_pleaf) {
-    ldcol(p, unsigned(hslot) * 512u + unsigned(hvox), in.H);
-  } else {
-#pragma unroll
-    for (int z = 0; z < 8; ++z) in.H.v[z] = T(0);
-  }
-  const int zs0 = fs[4], zs1 = fs[5];
-  const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
+  static_assert(std::is_same<T, float>::value, "the pipelined kernels take fp32 vectors");
+  ldcol(p, slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox), in.H);
+  const unsigned z0 = slot_or_null(fs[4], a.n_pleaf), z1 = slot_or_null(fs[5], a.n_pleaf);
   if constexpr (ZD) {
-    in.zm = zv0 ? ldv(p + (unsigned(zs0) * 512u + unsigned(h.c) + 7u)) : T(0);
-    in.zp = zv1 ? ldv(p + (unsigned(zs1) * 512u + unsigned(h.c))) : T(0);
-    return;
+    in.zm = ldv(p + (z0 * 512u + unsigned(h.c) + 7u));
+    in.zp = ldv(p + (z1 * 512u + unsigned(h.c)));
+  } else {
+    const T* zfp = static_cast<const T*>(a.zf) + (128u * unsigned(qcur) + unsigned(h.fidx));
+    in.zm = ldv(zfp + (z0 * 384u + 64u));
+    in.zp = ldv(zfp + z1 * 384u);
   }
-  const T* zfp = static_cast<const T*>(a.zf) + (128u * unsigned(qcur) + unsigned(h.fidx));
-  in.zm = zv0 ? ldv(zfp + (unsigned(zs0) * 384u + 64u)) : T(0);
-  in.zp = zv1 ? ldv(zfp + unsigned(zs1) * 384u) : T(0);
 }
 
 template <typename T, bool ZD>
@@ -1661,297 +1352,6 @@ __global__ void __launch_bounds__(kHotThreads, 4)
   }
   PartT<DM> v[2] = {drr.pvalue(), drz.pvalue()};
   put_partials<DM, 2>(a, 0, v);
-}
-
-// ---- persistent PCG loop (cooperative launch) ------------------------------
-// All iterations in one launch: every CTA stays resident (cooperative launch)
-// and keeps its half leaves for the whole solve; the two grid-wide steps of
-// an iteration (p.Ap before alpha, r.r and r.z before beta) are a grid
-// barrier whose last-arriving CTA sums the per-CTA partials in a fixed order
-// (deterministic) and publishes the totals, so every CTA forms the same
-// alpha, beta and stop decision.  Loads of vectors other CTAs wrote in this
-// launch (halo columns, z-face planes) go to L2; a warp's own columns were
-// written by that warp, so they may use L1.  Each barrier wait is bounded:
-// past ~2^24 polls the CTA records FSIM_ERR_TIMEOUT and the solve ends.
-constexpr unsigned kBarrierPolls = 1u << 24;
-
-template <int DM, int NV>
-__device__ bool grid_reduce_sync(double (&v)[NV], double (&tot)[NV], const PcgArgs& a,
-                                 unsigned& gen) {
-  __shared__ int s_last, s_err;
-  __shared__ double s_res[NV];
-  block_sum<DM, NV, kHotThreads>(v);
-  PcgScalars* sc = a.sc;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) a.part[k * a.maxb + blockIdx.x] = v[k];
-    __threadfence();
-    s_last = atomicAdd(&sc->bar_count, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (s_last) {
-    __threadfence();
-    double acc[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      const double* pk = a.part + k * a.maxb;
-      if (DM == 0) {
-        float x = 0.f;
-        for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += kHotThreads * 8) {
-          float t[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const int i = i0 + u * kHotThreads;
-            t[u] = i < int(gridDim.x) ? float(__ldcg(pk + i)) : 0.f;
-          }
-#pragma unroll
-          for (int u = 0; u < 8; ++u) x = __fadd_rn(x, t[u]);
-        }
-        acc[k] = double(x);
-      } else {
-        double x = 0.0;
-        for (int i0 = threadIdx.x; i0 < int(gridDim.x); i0 += kHotThreads * 8) {
-          double t[8];
-#pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const int i = i0 + u * kHotThreads;
-            t[u] = i < int(gridDim.x) ? __ldcg(pk + i) : 0.0;
-          }
-#pragma unroll
-          for (int u = 0; u < 8; ++u) x += t[u];
-        }
-        acc[k] = x;
-      }
-    }
-    block_sum<DM, NV, kHotThreads>(acc);
-    if (threadIdx.x == 0) {
-#pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        s_res[k] = acc[k];
-        sc->bar_tot[k] = acc[k];
-      }
-      sc->bar_count = 0u;
-      __threadfence();
-      atomicExch(&sc->bar_gen, gen + 1u);
-      s_err = __ldcg(&sc->bar_err) != 0u;
-    }
-  } else if (threadIdx.x == 0) {
-    volatile unsigned* g = &sc->bar_gen;
-    unsigned polls = 0;
-    while (*g == gen && polls < kBarrierPolls) {
-      __nanosleep(32);
-      ++polls;
-    }
-    const bool timed_out = *g == gen;
-    __threadfence();
-    if (timed_out) {
-      atomicExch(&sc->bar_err, 1u);
-    } else {
-#pragma unroll
-      for (int k = 0; k < NV; ++k) s_res[k] = __ldcg(&sc->bar_tot[k]);
-    }
-    s_err = timed_out || __ldcg(&sc->bar_err) != 0u;
-  }
-  __syncthreads();  // s_err is uniform across the CTA from here
-  ++gen;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = s_res[k];
-  return s_err == 0;
-}
-
-// p_j of the warp's half leaves, their p.Ap (one spmv phase)
-template <typename T, int DM>
-__device__ __forceinline__ void loop_spmv(const PcgArgs& a, Tile<T>& tile, const DiagInv<T>* tab,
-                                          int par, T beta, int hw0, int hstride, Dot<DM>& dp) {
-  const int lane = threadIdx.x & 31;
-  const T* r = static_cast<const T*>(a.r);
-  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
-  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
-  const int qold = 1 + (par ^ 1), qnew = 1 + par;
-  const T* zf = static_cast<const T*>(a.zf);
-  const int nhw = 2 * a.n_pleaf;
-  for (int hw = hw0; hw < nhw; hw += hstride) {
-    int fs[6];
-    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
-    const HalfLeaf h = half_pos(hw, lane);
-    const int64_t o = int64_t(h.s) * 512 + h.c;
-    const uint2 f = ldflags(a.flags, o);
-    Col<T> rc, pc, hr, hp;
-    ldcol(r, o, rc);
-    ldcol(pold, o, pc);
-    int hslot, hvox;
-    halo_col(h, fs, hslot, hvox);
-    const bool hv = hslot >= 0 && hslot < a.n_pleaf;
-    uint2 hf = make_uint2(0u, 0u);
-    if (hv) {
-      const int64_t hb = int64_t(hslot) * 512 + hvox;
-      hf = ldflags(a.flags, hb);
-      ldcol_cg(r, hb, hr);
-      ldcol_cg(pold, hb, hp);
-    } else {
-#pragma unroll
-      for (int z = 0; z < 8; ++z) hr.v[z] = hp.v[z] = T(0);
-    }
-    const int zs0 = fs[4], zs1 = fs[5];
-    const bool zv0 = zs0 >= 0 && zs0 < a.n_pleaf, zv1 = zs1 >= 0 && zs1 < a.n_pleaf;
-    const int64_t zo0 = int64_t(zv0 ? zs0 : 0) * 384 + 64 + h.fidx;
-    const int64_t zo1 = int64_t(zv1 ? zs1 : 0) * 384 + h.fidx;
-    const uint8_t zf0 = zv0 ? a.zff[int64_t(zs0) * 128 + 64 + h.fidx] : uint8_t(0);
-    const uint8_t zf1 = zv1 ? a.zff[int64_t(zs1) * 128 + h.fidx] : uint8_t(0);
-    const T zr0 = zv0 ? __ldcg(zf + zo0) : T(0), zr1 = zv1 ? __ldcg(zf + zo1) : T(0);
-    const T zq0 = zv0 ? __ldcg(zf + zo0 + 128 * qold) : T(0);
-    const T zq1 = zv1 ? __ldcg(zf + zo1 + 128 * qold) : T(0);
-    Col<T> P, H;
-#pragma unroll
-    for (int z = 0; z < 8; ++z) {
-      P.v[z] = pnew_of<T>(tab, fbyte(f, z), rc.v[z], pc.v[z], beta);
-      H.v[z] = pnew_of<T>(tab, fbyte(hf, z), hr.v[z], hp.v[z], beta);
-    }
-    const T zm = pnew_of<T>(tab, zf0, zr0, zq0, beta);
-    const T zp = pnew_of<T>(tab, zf1, zr1, zq1, beta);
-    stcol(pnew, o, P);
-    {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + 128 * qnew + h.fidx;
-      zw[0] = P.v[0];
-      zw[64] = P.v[7];
-    }
-    __syncwarp();
-    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
-    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
-    __syncwarp();
-    Col<T> ap;
-    stencil_col<T>(tile, tab, h.lx, h.cy, P, f, zm, zp, ap);
-#pragma unroll
-    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
-  }
-}
-
-// x += alpha p, r -= alpha A p, r.r and r.z (one update phase)
-template <typename T, int DM>
-__device__ __forceinline__ void loop_update(const PcgArgs& a, Tile<T>& tile,
-                                            const DiagInv<T>* tab, int par, T alpha, int hw0,
-                                            int hstride, Dot<DM>& drr, Dot<DM>& drz) {
-  const int lane = threadIdx.x & 31;
-  const T* p = static_cast<const T*>(par ? a.p1 : a.p0);
-  T* x = static_cast<T*>(a.x);
-  T* r = static_cast<T*>(a.r);
-  const int qcur = 1 + par;
-  const T nalpha = -alpha;
-  const int nhw = 2 * a.n_pleaf;
-  for (int hw = hw0; hw < nhw; hw += hstride) {
-    int fs[6];
-    face_slots(face_slot_lane(a.nbr, hw >> 1, lane), fs);
-    const HalfLeaf h = half_pos(hw, lane);
-    const int64_t o = int64_t(h.s) * 512 + h.c;
-    const uint2 f = ldflags(a.flags, o);
-    Col<T> P, H, xc, rc;
-    ldcol(p, o, P);
-    ldcol(x, o, xc);
-    ldcol(r, o, rc);
-    int hslot, hvox;
-    halo_col(h, fs, hslot, hvox);
-    if (hslot >= 0 && hslot < a.n_pleaf) {
-      ldcol_cg(p, int64_t(hslot) * 512 + hvox, H);
-    } else {
-#pragma unroll
-      for (int z = 0; z < 8; ++z) H.v[z] = T(0);
-    }
-    const int zs0 = fs[4], zs1 = fs[5];
-    const T* zfp = static_cast<const T*>(a.zf) + 128 * qcur + h.fidx;
-    const T zm = (zs0 >= 0 && zs0 < a.n_pleaf) ? __ldcg(zfp + int64_t(zs0) * 384 + 64) : T(0);
-    const T zp = (zs1 >= 0 && zs1 < a.n_pleaf) ? __ldcg(zfp + int64_t(zs1) * 384) : T(0);
-    __syncwarp();
-    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
-    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
-    __syncwarp();
-    Col<T> ap;
-    stencil_col<T>(tile, tab, h.lx, h.cy, P, f, zm, zp, ap);
-#pragma unroll
-    for (int z = 0; z < 8; ++z) {
-      const uint8_t g = fbyte(f, z);
-      xc.v[z] = tadd(tmul(alpha, P.v[z]), xc.v[z]);
-      rc.v[z] = tadd(tmul(nalpha, ap.v[z]), rc.v[z]);
-      drr.add(rc.v[z], rc.v[z]);
-      drz.add(rc.v[z], tmul(tab[g & 15].inv, rc.v[z]));
-    }
-    stcol(x, o, xc);
-    stcol(r, o, rc);
-    {
-      T* zw = static_cast<T*>(a.zf) + int64_t(h.s) * 384 + h.fidx;
-      zw[0] = rc.v[0];
-      zw[64] = rc.v[7];
-    }
-  }
-}
-
-template <typename T, int DM>
-__global__ void __launch_bounds__(kHotThreads, hot_minb<T>())
-    k_pcg_loop(const __grid_constant__ PcgArgs a) {
-  __shared__ Tile<T> tiles[kHotThreads / 32];
-  __shared__ DiagInv<T> tab[16];
-  __shared__ unsigned s_gen;
-  PcgScalars* sc = a.sc;
-  fill_diag_table<T>(tab);
-  if (threadIdx.x == 0) s_gen = *reinterpret_cast<volatile unsigned*>(&sc->bar_gen);
-  __syncthreads();
-  unsigned gen = s_gen;
-  Tile<T>& tile = tiles[threadIdx.x >> 5];
-  const int wpb = kHotThreads / 32;
-  const int hw0 = blockIdx.x * wpb + (threadIdx.x >> 5), hstride = gridDim.x * wpb;
-  const bool fp32 = sc->fp32 != 0;
-  int it = sc->iter, done = sc->done, status = sc->status;
-  const int max_iter = sc->max_iter;
-  double rz = sc->rz, rr = sc->rr, beta = sc->beta, alpha = 0.0, pAp = 0.0, rz_old = sc->rz_old;
-  bool ok = true;
-  while (!done) {
-    const int par = it & 1;
-    {
-      Dot<DM> dp;
-      loop_spmv<T, DM>(a, tile, tab, par, T(beta), hw0, hstride, dp);
-      double v[1] = {dp.value()}, tot[1];
-      if (!(ok = grid_reduce_sync<DM, 1>(v, tot, a, gen))) break;
-      pAp = fp32 ? double(float(tot[0])) : tot[0];
-      alpha = fp32 ? double(__fdiv_rn(float(rz), float(pAp))) : rz / pAp;
-      if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
-        status = FSIM_ERR_BREAKDOWN;
-        done = 1;
-        break;
-      }
-    }
-    {
-      Dot<DM> drr, drz;
-      loop_update<T, DM>(a, tile, tab, par, T(alpha), hw0, hstride, drr, drz);
-      double v[2] = {drr.value(), drz.value()}, tot[2];
-      if (!(ok = grid_reduce_sync<DM, 2>(v, tot, a, gen))) break;
-      rr = fp32 ? double(float(tot[0])) : tot[0];
-      rz_old = rz;
-      rz = fp32 ? double(float(tot[1])) : tot[1];
-      beta = fp32 ? double(__fdiv_rn(float(rz), float(rz_old))) : rz / rz_old;
-      ++it;
-      if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
-        status = FSIM_ERR_BREAKDOWN;
-        done = 1;
-      } else {
-        done = (it >= max_iter) || converged(sc, rr);
-      }
-    }
-  }
-  if (!ok) {
-    status = FSIM_ERR_TIMEOUT;
-    done = 1;
-  }
-  // every CTA holds the same scalars; one writes them back
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    sc->iter = it;
-    sc->done = done;
-    sc->status = status;
-    sc->rr = rr;
-    sc->rz = rz;
-    sc->rz_old = rz_old;
-    sc->alpha = alpha;
-    sc->beta = beta;
-    sc->pAp = pAp;
-  }
 }
 
 // MIXED: x64 += d (inner solution); d is the fp32 x of the inner solve.
@@ -2054,15 +1454,11 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
     pres[o] = float(x[o]);
 }
 
-// The hot kernel pair of a solve: the bulk-copy staged spmv (FP32 dots,
-// FSIM_PCG_TMA=1), the register-pipelined pair (fp32 vectors), or the plain
-// pair (fp64 vectors, or FSIM_PCG_PIPE=0).
+// The hot kernel pair of a solve: the register-pipelined pair (fp32
+// vectors), or the plain pair (fp64 vectors, or FSIM_PCG_PIPE=0).
 template <typename T, int DM>
 void* spmv_kernel(const fsim_sim* s, bool zd) {
   if constexpr (std::is_same<T, float>::value) {
-    if constexpr (DM == 0) {
-      if (s->use_pipe && s->use_tma) return reinterpret_cast<void*>(k_pcg_spmv_tma<DM>);
-    }
     if (s->use_pipe)
       return zd ? reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM, true>)
                 : reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM, false>);
@@ -2080,11 +1476,10 @@ void* update_kernel(const fsim_sim* s, bool zd) {
 }
 // Large systems: the pipelined kernels read z-face neighbours from the
 // vectors (L2 hits) instead of the published planes, which no longer fit in
-// L2 and cost about 4 B of DRAM traffic per unknown and iteration.  The
-// spmv's bulk-copy variant always uses the planes.
+// L2 and cost about 4 B of DRAM traffic per unknown and iteration.
 template <typename T>
 bool use_zdirect(const fsim_sim* s, int n_pleaf) {
-  return std::is_same<T, float>::value && s->use_pipe && !s->use_tma &&
+  return std::is_same<T, float>::value && s->use_pipe &&
          (s->zdirect > 0 || (s->zdirect < 0 && n_pleaf > kZDirectLeaves));
 }
 int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
@@ -2109,12 +1504,16 @@ int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
 // Pass length: each pass costs about 4 us of graph overhead, and the last
 // pass runs up to pass - 1 iterations of launches that return at once (about
 // 5 us each).  For I iterations the sum is smallest near pass = sqrt(1.7 I),
-// so the pass length follows the handle's previous solve: 8 iterations up to
-// about 150, 16 up to about 600, then 32 (even, so that a pass leaves the
-// launch parity where it found it).  FSIM_PCG_PASS_ITERS fixes it instead.
+// so the pass length follows the longest graph-loop segment of the handle's
+// previous solve (a MIXED solve runs several segments, and its last one is
+// often short): 8 iterations up to about 150, 16 up to about 600, then 32
+// (even, so that a pass leaves the launch parity where it found it).  FSIM_PCG_PASS_ITERS fixes it instead
+// (an even count; an odd one would swap the p buffers of every later pass).
 #ifndef FSIM_PCG_PASS_ITERS
 #define FSIM_PCG_PASS_ITERS 0
 #endif
+static_assert(FSIM_PCG_PASS_ITERS >= 0 && FSIM_PCG_PASS_ITERS % 2 == 0,
+              "FSIM_PCG_PASS_ITERS must be even: a pass must keep the launch parity");
 int pass_iters_for(const fsim_sim* s) {
   if (FSIM_PCG_PASS_ITERS > 0) return FSIM_PCG_PASS_ITERS;
   const double p = std::sqrt(1.7 * double(s->pcg_last_iters));
@@ -2220,35 +1619,6 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
                                           s->max_blocks, kMaxHotGrid}));
-  if (s->use_coop && !s->profiling) {
-    // one cooperative launch runs every iteration (setup has already run)
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pcg_loop<T, DM>, kHotThreads, 0);
-    const int cgrid = std::min({std::max(occ, 0) * s->num_sms, (2 * a.n_pleaf + wpb - 1) / wpb,
-                                s->max_blocks});
-    if (cgrid > 0) {
-      PcgArgs ca = a;
-      ca.cond = 0;
-      void* args[] = {&ca};
-      ProfScope ps(s, nm_spmv);
-      LoopTimer lt(s);
-      cudaError_t e = cudaLaunchCooperativeKernel(reinterpret_cast<void*>(k_pcg_loop<T, DM>),
-                                                  dim3(unsigned(cgrid)), dim3(kHotThreads), args,
-                                                  0, s->stream);
-      if (e == cudaSuccess) {
-        lt.stop();
-        s->launches += 1;
-        FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
-                                   s->stream));
-        FSIM_CK(s, cudaStreamSynchronize(s->stream));
-        if (s->h_sc->status == FSIM_ERR_TIMEOUT)
-          return fail(s, FSIM_ERR_TIMEOUT, "PCG grid barrier timed out");
-        return FSIM_OK;
-      }
-      cudaGetLastError();  // refused (e.g. not co-resident): use the graph loop
-      s->use_coop = false;
-    }
-  }
   const int it0 = setup ? 0 : s->h_sc->iter;  // iterations before this segment
   if (s->use_graphs && !s->profiling) {
     LoopTimer lt(s);
@@ -2257,7 +1627,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     // which prefetch before their wait; the others wait at their first
     // instruction, and their early-launched CTAs only hold SM slots (the
     // FP64 solve measured 20% slower with them).
-    const bool pdl = s->use_pdl && std::is_same<T, float>::value && s->use_pipe && !s->use_tma;
+    const bool pdl = s->use_pdl && std::is_same<T, float>::value && s->use_pipe;
     const int pass_iters = pass_iters_for(s);
     if (pdl) {
       rc = run_graph_loop<T, DM>(s, a, wgrid, par0, true, pass_iters);
@@ -2274,8 +1644,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       // n / pass_iters + 1 passes ran
       const int64_t n = std::max(s->h_sc->iter - it0, 0);
       s->launches += 2 * pass_iters * (n / pass_iters + 1);
-      s->pcg_last_iters = int(std::min<int64_t>(n, 1 << 30));
-      if (s->h_sc->bar_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG stage copy did not complete");
+      s->pcg_seg_max = std::max(s->pcg_seg_max, int(std::min<int64_t>(n, 1 << 30)));
       return FSIM_OK;
     }
     s->use_graphs = false;  // fall back for the rest of this handle's life
@@ -2288,7 +1657,7 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                s->stream));
     FSIM_CK(s, cudaStreamSynchronize(s->stream));
-    if (s->h_sc->done || s->h_sc->bar_err) break;
+    if (s->h_sc->done) break;
     for (int c = 0; c < chunk; ++c, ++launched) {
       a.par = int(launched & 1);
       int rc = launch_hot(s, nm_spmv, fn_spmv, wgrid, a);
@@ -2298,7 +1667,6 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     if (chunk < 64) chunk *= 2;
   }
   lt.stop();
-  if (s->h_sc->bar_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG stage copy did not complete");
   return FSIM_OK;
 }
 
@@ -2327,6 +1695,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
   int rc = ensure_pcg_vectors(s, prm->precision);
   if (rc) return rc;
   s->pcg_loop_ms = 0.0;
+  s->pcg_seg_max = 0;
   const int grid = std::max(1, std::min(s->n_pleaf, s->max_blocks));
   PcgArgs a;
   memset(&a, 0, sizeof(a));
@@ -2437,6 +1806,7 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
                 unsigned(std::min<int64_t>((nvec + 255) / 256, 4096)), 256, 0, s->x64, s->pres,
                 nvec);
   }
+  if (s->pcg_seg_max > 0) s->pcg_last_iters = s->pcg_seg_max;
   if (st) {
     st->iterations = total_it;
     st->refinements = refinements;

@@ -379,8 +379,11 @@ int fsim_download_leaves(fsim_t* sim, int32_t* origins, int64_t capacity,
  * scratch is a fixed file-scope device array (4 KB + a counter) that every
  * GPU loading the library holds until exit.  The first call on a device
  * looks up that array's address (cudaGetSymbolAddress) with the device
- * current, so make the first call before any stream capture.  All calls on
- * a device share the scratch: calls that overlap on the GPU race.
+ * current, so make the first call before any stream capture.  The address
+ * is kept per device for the life of the process: after cudaDeviceReset (a
+ * new primary context) it is stale, so do not call this across a reset.
+ * All calls on a device share the scratch: calls that overlap on the GPU
+ * race.
  * Returns FSIM_ERR_CAPACITY when a dimension exceeds 1024 (the maximum),
  * FSIM_ERR_INVALID for a null pointer or a dimension below 8. */
 int fsim_cfl_noalloc(const float* vel, const uint8_t* active, const int32_t dims[3],

@@ -1,7 +1,9 @@
 // oracle.cc -- CPU restatement of the reference FLIP step (TEST INFRASTRUCTURE).
 //
 // Loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-// leg.  Built strict: -O2 -ffp-contract=off, no fast-math, single thread.
+// leg.  Built strict: -O2 -ffp-contract=off, no fast-math.  One thread by
+// default; orc_set_threads spreads the loops whose results do not depend on
+// the thread count over a pool (see Pool below).
 // Every function cites the reference code it restates (paths relative to the
 // schinmayee/fluid-sim-lb project).  Parity status: unpinned against the
 // reference binary (it cannot be built here); pinned by known-answer tests.
@@ -12,6 +14,10 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -19,6 +25,87 @@ namespace {
 enum { AIR = 0, FLUID = 1, SOLID = 2 };
 
 inline int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
+
+// ---- host threads -----------------------------------------------------------
+// A pool for loops whose iterations write disjoint elements (per particle,
+// per leaf, per matrix row, per vector entry), for the chunk sums of the
+// PCG dots, whose chunk totals are then added in chunk order, and for the
+// four lane sums of p.Ap.  Every result is therefore bit-identical for any
+// thread count; the P2G leaf write-back, whose order spans the whole grid,
+// stays serial.  bench.py's reference arm uses it; the tests run one thread.
+class Pool {
+ public:
+  ~Pool() { resize(1); }
+  int size() const { return nthreads_; }
+  void resize(int n) {
+    n = std::max(1, std::min(n, 256));
+    if (n == nthreads_) return;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : workers_) t.join();
+    workers_.clear();
+    stop_ = false;
+    nthreads_ = n;
+    const uint64_t g0 = gen_;
+    for (int w = 1; w < n; ++w) workers_.emplace_back([this, w, g0] { loop(w, g0); });
+  }
+  // job(t) for t in [0, size()): thread 0 is the caller
+  void run(const std::function<void(int)>& job) {
+    if (nthreads_ == 1) { job(0); return; }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &job;
+      pending_ = nthreads_ - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    job(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [this] { return pending_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void loop(int w, uint64_t seen) {
+    for (;;) {
+      const std::function<void(int)>* job;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        job = job_;
+      }
+      (*job)(w);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--pending_ == 0) done_cv_.notify_one();
+    }
+  }
+  int nthreads_ = 1;
+  std::vector<std::thread> workers_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* job_ = nullptr;
+  uint64_t gen_ = 0;
+  int pending_ = 0;
+  bool stop_ = false;
+};
+Pool g_pool;
+
+// f(begin, end) over contiguous ranges of [0, n), one per pool thread.
+template <class F>
+void par_for(size_t n, F&& f) {
+  const int T = g_pool.size();
+  if (T == 1 || n < 4096) { f(size_t(0), n); return; }
+  g_pool.run([&](int t) {
+    const size_t b = n * size_t(t) / size_t(T), e = n * size_t(t + 1) / size_t(T);
+    if (b < e) f(b, e);
+  });
+}
 
 // ---- seeding draw: SplitMix64 finaliser (Steele, Lea, Flood 2014) ----------
 inline uint64_t mix64(uint64_t z) {
@@ -171,29 +258,57 @@ void reorder_by_key(orc_sim* s) {
   const size_t n = s->keys.size();
   std::vector<uint32_t> idx(n), tmp(n), kin(s->keys), kout(n);
   for (size_t i = 0; i < n; ++i) idx[i] = uint32_t(i);
+  // each pool thread counts and scatters one contiguous block; block t's
+  // entries of a bucket go after blocks 0..t-1's, so every pass is stable
+  const int T = n < 65536 ? 1 : g_pool.size();
+  std::vector<size_t> cnt(size_t(T) * 256);
   for (int shift = 0; shift < 32; shift += 8) {
-    size_t cnt[257] = {0};
-    for (size_t i = 0; i < n; ++i) cnt[((kin[i] >> shift) & 255u) + 1]++;
-    for (int b = 0; b < 256; ++b) cnt[b + 1] += cnt[b];
-    for (size_t i = 0; i < n; ++i) {
-      size_t d = cnt[(kin[i] >> shift) & 255u]++;
-      kout[d] = kin[i];
-      tmp[d] = idx[i];
-    }
+    std::fill(cnt.begin(), cnt.end(), size_t(0));
+    auto block = [&](int t, size_t& b, size_t& e) {
+      b = n * size_t(t) / size_t(T);
+      e = n * size_t(t + 1) / size_t(T);
+    };
+    auto count = [&](int t) {
+      size_t b, e;
+      block(t, b, e);
+      size_t* c = &cnt[size_t(t) * 256];
+      for (size_t i = b; i < e; ++i) c[(kin[i] >> shift) & 255u]++;
+    };
+    if (T == 1) count(0); else g_pool.run(count);
+    size_t run = 0;
+    for (int d = 0; d < 256; ++d)
+      for (int t = 0; t < T; ++t) {
+        const size_t c = cnt[size_t(t) * 256 + d];
+        cnt[size_t(t) * 256 + d] = run;
+        run += c;
+      }
+    auto scatter = [&](int t) {
+      size_t b, e;
+      block(t, b, e);
+      size_t* c = &cnt[size_t(t) * 256];
+      for (size_t i = b; i < e; ++i) {
+        const size_t d = c[(kin[i] >> shift) & 255u]++;
+        kout[d] = kin[i];
+        tmp[d] = idx[i];
+      }
+    };
+    if (T == 1) scatter(0); else g_pool.run(scatter);
     kin.swap(kout);
     idx.swap(tmp);
   }
   std::vector<float> p2(3 * n), v2(3 * n), g2(3 * n);
   std::vector<int32_t> c2(3 * n);
-  for (size_t i = 0; i < n; ++i) {
-    size_t o = idx[i];
-    for (int d = 0; d < 3; ++d) {
-      p2[3 * i + d] = s->pos[3 * o + d];
-      v2[3 * i + d] = s->vel_p[3 * o + d];
-      g2[3 * i + d] = s->gvel[3 * o + d];
-      c2[3 * i + d] = s->cell[3 * o + d];
+  par_for(n, [&](size_t i0, size_t i1) {
+    for (size_t i = i0; i < i1; ++i) {
+      size_t o = idx[i];
+      for (int d = 0; d < 3; ++d) {
+        p2[3 * i + d] = s->pos[3 * o + d];
+        v2[3 * i + d] = s->vel_p[3 * o + d];
+        g2[3 * i + d] = s->gvel[3 * o + d];
+        c2[3 * i + d] = s->cell[3 * o + d];
+      }
     }
-  }
+  });
   s->pos.swap(p2); s->vel_p.swap(v2); s->gvel.swap(g2); s->cell.swap(c2);
   s->keys.swap(kin);
 }
@@ -329,50 +444,76 @@ struct PCG {
     std::vector<T> b(R), x(R, T(0)), r(R), z(R), p(R), Ap(R);
     static const int off[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0},
                                   {0, 1, 0},  {0, 0, -1}, {0, 0, 1}};
-    size_t row = 0;
-    for (int i = 0; i < n[0]; ++i)
-      for (int j = 0; j < n[1]; ++j)
-        for (int k = 0; k < n[2]; ++k) {
-          if (mget(s, i, j, k) != FLUID) continue;
-          T diag = 0;
-          std::vector<std::pair<int32_t, T>> ent;
-          for (int q = 0; q < 6; ++q) {
-            int a = i + off[q][0], bb = j + off[q][1], c = k + off[q][2];
-            int m = mget(s, a, bb, c);
-            if (m == FLUID || m == AIR) diag += T(1);
-            if (m == FLUID) ent.push_back({idx[s->D.idx(a, bb, c)], T(-1)});
-          }
-          ent.push_back({int32_t(row), diag});
-          std::sort(ent.begin(), ent.end(),
-                    [](const std::pair<int32_t, T>& u, const std::pair<int32_t, T>& v) {
-                      return u.first < v.first;
-                    });
-          for (size_t e = 0; e < ent.size(); ++e) {
-            cols[7 * row + e] = ent[e].first;
-            vals[7 * row + e] = ent[e].second;
-          }
-          invd[row] = T(1.0 / double(diag));
-          b[row] = T(fget(s, s->div, s->div_on, i, j, k));
-          ++row;
+    par_for(R, [&](size_t r0, size_t r1) {
+      for (size_t row = r0; row < r1; ++row) {
+        const size_t cx = cells[row];
+        const int i = int(cx / (size_t(s->D.s[1]) * s->D.s[2])) - 2;
+        const int j = int((cx / size_t(s->D.s[2])) % size_t(s->D.s[1])) - 2;
+        const int k = int(cx % size_t(s->D.s[2])) - 2;
+        T diag = 0;
+        std::pair<int32_t, T> ent[7];
+        int ne = 0;
+        for (int q = 0; q < 6; ++q) {
+          int a = i + off[q][0], bb = j + off[q][1], c = k + off[q][2];
+          int m = mget(s, a, bb, c);
+          if (m == FLUID || m == AIR) diag += T(1);
+          if (m == FLUID) ent[ne++] = {idx[s->D.idx(a, bb, c)], T(-1)};
         }
-    auto spmv = [&](const std::vector<T>& in, std::vector<T>& out) {
-      for (size_t q = 0; q < R; ++q) {
-        T acc = 0;
-        for (int e = 0; e < 7 && cols[7 * q + e] >= 0; ++e)
-          acc += vals[7 * q + e] * in[cols[7 * q + e]];
-        out[q] = acc;
+        ent[ne++] = {int32_t(row), diag};
+        std::sort(ent, ent + ne,
+                  [](const std::pair<int32_t, T>& u, const std::pair<int32_t, T>& v) {
+                    return u.first < v.first;
+                  });
+        for (int e = 0; e < ne; ++e) {
+          cols[7 * row + e] = ent[e].first;
+          vals[7 * row + e] = ent[e].second;
+        }
+        invd[row] = T(1.0 / double(diag));
+        b[row] = T(fget(s, s->div, s->div_on, i, j, k));
       }
+    });
+    auto spmv = [&](const std::vector<T>& in, std::vector<T>& out) {
+      par_for(R, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q) {
+          T acc = 0;
+          for (int e = 0; e < 7 && cols[7 * q + e] >= 0; ++e)
+            acc += vals[7 * q + e] * in[cols[7 * q + e]];
+          out[q] = acc;
+        }
+      });
     };
+    // pcg::Vector<T>::dot of OpenVDB 4.0.1 (third party, absent here) sums
+    // contiguous ranges of the vector in parallel and then adds the range
+    // totals; its exact split is not pinned.  Restated as kDotChunks equal
+    // contiguous chunks (the last one takes the remainder), each summed
+    // serially in T, chunk totals added in chunk order.  The split matters:
+    // on the first system of the 256^3 dam break (4.02 M rows) a single
+    // serial sum needs 1134 iterations to relative 1e-5, 100 chunks 881.
+    constexpr size_t kDotChunks = 100;
+    std::vector<T> chunk_sum(kDotChunks);
     auto dot = [&](const std::vector<T>& u, const std::vector<T>& v) {
+      const size_t sz = R / kDotChunks;
+      par_for(kDotChunks, [&](size_t c0, size_t c1) {
+        for (size_t c = c0; c < c1; ++c) {
+          const size_t e = (c + 1 == kDotChunks) ? R : (c + 1) * sz;
+          T a = 0;
+          for (size_t q = c * sz; q < e; ++q) a += u[q] * v[q];
+          chunk_sum[c] = a;
+        }
+      });
       T acc = 0;
-      for (size_t q = 0; q < R; ++q) acc += u[q] * v[q];
+      for (size_t c = 0; c < kDotChunks; ++c) acc += chunk_sum[c];
       return acc;
     };
     // PreparePCGSolver: r = b - A x; z = M^-1 r; p = z; rz; rr
     spmv(x, Ap);
-    for (size_t q = 0; q < R; ++q) r[q] = b[q] - Ap[q];
-    for (size_t q = 0; q < R; ++q) z[q] = invd[q] * r[q];
-    p = z;
+    par_for(R, [&](size_t q0, size_t q1) {
+      for (size_t q = q0; q < q1; ++q) {
+        r[q] = b[q] - Ap[q];
+        z[q] = invd[q] * r[q];
+        p[q] = z[q];
+      }
+    });
     T rz = dot(r, z), rr = dot(r, r);
     const T bb = dot(b, b);
     const T thr = T(threshold);
@@ -388,21 +529,48 @@ struct PCG {
     while (!done()) {
       // ComputeLocal1
       spmv(p, Ap);
-      T pAp = 0;
-      for (size_t q = 0; q < R; ++q) pAp += p[q] * Ap[q];
+      // The reference's own loop (common/solver.cc:304-307): one running sum
+      // in source, built -Ofast (makeinclude/flags.mk:6), which lets the
+      // compiler vectorise the reduction.  Restated as 4-wide vector code
+      // sums it: lane l accumulates the terms q = l (mod 4) over the
+      // multiple-of-4 prefix, the lanes are added as (l0 + l2) + (l1 + l3),
+      // then the tail terms in order.  (A single running sum here, with the
+      // chunked dots above, diverges on the second system of the 256^3 dam
+      // break: p.Ap then carries far more rounding than r.z.)
+      const size_t R4 = R & ~size_t(3);
+      T lane[4] = {0, 0, 0, 0};
+      auto lane_sum = [&](size_t l) {
+        T a = 0;
+        for (size_t q = l; q < R4; q += 4) a += p[q] * Ap[q];
+        lane[l] = a;
+      };
+      if (g_pool.size() >= 4 && R4 >= 4096)
+        g_pool.run([&](int t) {
+          for (size_t l = size_t(t); l < 4; l += size_t(g_pool.size())) lane_sum(l);
+        });
+      else
+        for (size_t l = 0; l < 4; ++l) lane_sum(l);
+      T pAp = (lane[0] + lane[2]) + (lane[1] + lane[3]);
+      for (size_t q = R4; q < R; ++q) pAp += p[q] * Ap[q];
       // ComputeLocal2
       T alpha = rz / pAp;
       if (!(alpha <= T(1e5))) { status = 5; break; }
-      for (size_t q = 0; q < R; ++q) x[q] = alpha * p[q] + x[q];
-      for (size_t q = 0; q < R; ++q) r[q] = -alpha * Ap[q] + r[q];
-      for (size_t q = 0; q < R; ++q) z[q] = invd[q] * r[q];
+      par_for(R, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q) {
+          x[q] = alpha * p[q] + x[q];
+          r[q] = -alpha * Ap[q] + r[q];
+          z[q] = invd[q] * r[q];
+        }
+      });
       rr = dot(r, r);
       T rz_old = rz;
       rz = dot(r, z);
       // ComputeLocal3
       T beta = rz / rz_old;
       if (!(beta <= T(1e5))) { status = 5; ++it; break; }
-      for (size_t q = 0; q < R; ++q) p[q] = z[q] + beta * p[q];
+      par_for(R, [&](size_t q0, size_t q1) {
+        for (size_t q = q0; q < q1; ++q) p[q] = z[q] + beta * p[q];
+      });
       ++it;
     }
     if (status == 0 && mode == 1 && double(rr) > tol2bb) status = 4;
@@ -452,6 +620,9 @@ orc_sim* orc_create(const int32_t dims[3], int32_t boundary, float gravity,
 }
 
 void orc_destroy(orc_sim* s) { delete s; }
+
+void orc_set_threads(int32_t n) { g_pool.resize(n); }
+int32_t orc_get_threads(void) { return g_pool.size(); }
 
 void orc_add_solid_cuboid(orc_sim* s, const int32_t lo[3], const int32_t hi[3]) {
   // AddSolidCuboid, common/flip_simulation.cc:316-324: domain grown by 1,
@@ -597,19 +768,21 @@ void orc_move_particles(orc_sim* s, float dt) {
   // Particles::StepInGrid<VectorGrid,true,1,1>, particles.cc:479-546
   const size_t n = s->keys.size();
   const int* dims = s->D.n;
-  for (size_t i = 0; i < n; ++i) {
-    float* p = &s->pos[3 * i];
-    const float* g = &s->gvel[3 * i];
-    for (int d = 0; d < 3; ++d) p[d] = p[d] + g[d] * dt;
-    int id[3];
-    for (int d = 0; d < 3; ++d) id[d] = int(std::floor(p[d]));
-    for (int d = 0; d < 3; ++d)
-      if (id[d] < 0) { id[d] = 0; p[d] = 0.f; }
-    for (int d = 0; d < 3; ++d)
-      if (id[d] >= dims[d]) { id[d] = dims[d]; p[d] = float(dims[d]); }
-    for (int d = 0; d < 3; ++d) s->cell[3 * i + d] = id[d];
-    s->keys[i] = s->K.key(id[0], id[1], id[2]);
-  }
+  par_for(n, [&](size_t i0, size_t i1) {
+    for (size_t i = i0; i < i1; ++i) {
+      float* p = &s->pos[3 * i];
+      const float* g = &s->gvel[3 * i];
+      for (int d = 0; d < 3; ++d) p[d] = p[d] + g[d] * dt;
+      int id[3];
+      for (int d = 0; d < 3; ++d) id[d] = int(std::floor(p[d]));
+      for (int d = 0; d < 3; ++d)
+        if (id[d] < 0) { id[d] = 0; p[d] = 0.f; }
+      for (int d = 0; d < 3; ++d)
+        if (id[d] >= dims[d]) { id[d] = dims[d]; p[d] = float(dims[d]); }
+      for (int d = 0; d < 3; ++d) s->cell[3 * i + d] = id[d];
+      s->keys[i] = s->K.key(id[0], id[1], id[2]);
+    }
+  });
   reorder_by_key(s);
   orc_delete_particles_in_solids(s);
 }
@@ -648,15 +821,27 @@ void orc_transfer_particles_to_grid(orc_sim* s) {
   std::vector<size_t> st;
   leaf_ranges(s, st);
   const int S = 1000;
-  std::vector<float> vb(3 * S), wb(3 * S);
-  std::vector<uint8_t> mb(3 * S);
-  for (size_t l = 0; l + 1 < st.size(); ++l) {
+  const size_t nleaf = st.size() - 1;
+  // Each leaf's (8+2)^3 halo buffers are summed over its particles in list
+  // order, then added into the grid leaf by leaf in iteration order.  The
+  // buffers of a batch of leaves are filled by the pool (leaves are
+  // independent, and a leaf marks only its own cells FLUID); the write-back
+  // stays serial in leaf order, so the grid sums do not depend on the
+  // thread count.
+  const size_t batch = g_pool.size() == 1 ? 1 : 512;
+  std::vector<float> vb(batch * 3 * S), wb(batch * 3 * S);
+  std::vector<uint8_t> mb(batch * 3 * S);
+  std::vector<int> orgs(batch * 3);
+  auto fill = [&](size_t l, size_t slot) {
+    float* V = &vb[slot * 3 * S];
+    float* W = &wb[slot * 3 * S];
+    uint8_t* M = &mb[slot * 3 * S];
+    int* org = &orgs[slot * 3];
     const int32_t* c0 = &s->cell[3 * st[l]];
-    int org[3];
     for (int d = 0; d < 3; ++d) org[d] = floor_div(c0[d], 8) * 8 - 1;
-    std::fill(vb.begin(), vb.end(), 0.f);
-    std::fill(wb.begin(), wb.end(), 0.f);
-    std::fill(mb.begin(), mb.end(), 0);
+    std::fill(V, V + 3 * S, 0.f);
+    std::fill(W, W + 3 * S, 0.f);
+    std::fill(M, M + 3 * S, uint8_t(0));
     for (size_t q = st[l]; q < st[l + 1]; ++q) {
       const int* c = &s->cell[3 * q];
       if (c[0] >= 0 && c[0] < n[0] && c[1] >= 0 && c[1] < n[1] && c[2] >= 0 && c[2] < n[2])
@@ -672,35 +857,56 @@ void orc_transfer_particles_to_grid(orc_sim* s) {
           for (int dj = 0; dj < 2; ++dj)
             for (int dk = 0; dk < 2; ++dk) {
               int o = ((start[0] + di) * 10 + (start[1] + dj)) * 10 + (start[2] + dk);
-              vb[D * S + o] += w[di][dj][dk] * v[D];
-              wb[D * S + o] += w[di][dj][dk];
-              mb[D * S + o] = 1;
+              V[D * S + o] += w[di][dj][dk] * v[D];
+              W[D * S + o] += w[di][dj][dk];
+              M[D * S + o] = 1;
             }
       }
     }
+  };
+  auto write_back = [&](size_t slot) {
+    const float* V = &vb[slot * 3 * S];
+    const float* W = &wb[slot * 3 * S];
+    const uint8_t* M = &mb[slot * 3 * S];
+    const int* org = &orgs[slot * 3];
     for (int i = 0; i < 10; ++i)
       for (int j = 0; j < 10; ++j)
         for (int k = 0; k < 10; ++k) {
           int o = (i * 10 + j) * 10 + k;
-          if (!mb[o] && !mb[S + o] && !mb[2 * S + o]) continue;
+          if (!M[o] && !M[S + o] && !M[2 * S + o]) continue;
           int x = org[0] + i, y = org[1] + j, z = org[2] + k;
           Vec3f v = vget(s, s->vel, s->vel_on, x, y, z);
-          for (int D = 0; D < 3; ++D) v.v[D] = v.v[D] + vb[D * S + o];
+          for (int D = 0; D < 3; ++D) v.v[D] = v.v[D] + V[D * S + o];
           vset(s, s->vel, s->vel_on, x, y, z, v);
           Vec3f w = vget(s, s->weight, s->weight_on, x, y, z);
-          for (int D = 0; D < 3; ++D) w.v[D] = w.v[D] + wb[D * S + o];
+          for (int D = 0; D < 3; ++D) w.v[D] = w.v[D] + W[D * S + o];
           vset(s, s->weight, s->weight_on, x, y, z, w);
         }
+  };
+  for (size_t l0 = 0; l0 < nleaf; l0 += batch) {
+    const size_t nb = std::min(batch, nleaf - l0);
+    if (nb == 1) {
+      fill(l0, 0);
+    } else {
+      const int T = g_pool.size();
+      g_pool.run([&](int t) {
+        for (size_t b = nb * size_t(t) / size_t(T); b < nb * size_t(t + 1) / size_t(T); ++b)
+          fill(l0 + b, b);
+      });
+    }
+    for (size_t b = 0; b < nb; ++b) write_back(b);
   }
   // normalise every active face (THRESH 1e-5)
-  for (size_t x = 0; x < s->D.total; ++x) {
-    if (!s->vel_on[x]) continue;
-    for (int D = 0; D < 3; ++D) {
-      float ws = s->weight_on[x] ? s->weight[3 * x + D] : 0.f;
-      if (double(ws) < 1e-5) s->vel[3 * x + D] = 0.f;  // THRESH is a double literal
-      else s->vel[3 * x + D] = s->vel[3 * x + D] / ws;
+  par_for(s->D.total, [&](size_t x0, size_t x1) {
+    for (size_t x = x0; x < x1; ++x) {
+      if (!s->vel_on[x]) continue;
+      for (int D = 0; D < 3; ++D) {
+        float ws = s->weight_on[x] ? s->weight[3 * x + D] : 0.f;
+        if (double(ws) < 1e-5) s->vel[3 * x + D] = 0.f;  // THRESH is a double literal
+        else s->vel[3 * x + D] = s->vel[3 * x + D] / ws;
+      }
     }
-  }
+  });
 }
 
 void orc_apply_boundary_conditions(orc_sim* s) {
@@ -868,33 +1074,36 @@ void orc_update_particles_from_grid(orc_sim* s) {
   orc_extrapolate_to_boundary(s, 1);
   std::vector<size_t> st;
   leaf_ranges(s, st);
-  std::vector<float> vb(3000), db(3000);
-  for (size_t l = 0; l + 1 < st.size(); ++l) {
-    const int32_t* c0 = &s->cell[3 * st[l]];
-    int org[3];
-    for (int d = 0; d < 3; ++d) org[d] = floor_div(c0[d], 8) * 8 - 1;
-    for (int i = 0; i < 10; ++i)
-      for (int j = 0; j < 10; ++j)
-        for (int k = 0; k < 10; ++k) {
-          int o = (i * 10 + j) * 10 + k;
-          Vec3f v = vget(s, s->vel, s->vel_on, org[0] + i, org[1] + j, org[2] + k);
-          Vec3f dv = vget(s, s->vold, s->vold_on, org[0] + i, org[1] + j, org[2] + k);
-          for (int D = 0; D < 3; ++D) { vb[D * 1000 + o] = v.v[D]; db[D * 1000 + o] = dv.v[D]; }
+  // leaves are independent: each pool thread takes a contiguous range
+  par_for(st.size() - 1, [&](size_t l0, size_t l1) {
+    std::vector<float> vb(3000), db(3000);
+    for (size_t l = l0; l < l1; ++l) {
+      const int32_t* c0 = &s->cell[3 * st[l]];
+      int org[3];
+      for (int d = 0; d < 3; ++d) org[d] = floor_div(c0[d], 8) * 8 - 1;
+      for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 10; ++j)
+          for (int k = 0; k < 10; ++k) {
+            int o = (i * 10 + j) * 10 + k;
+            Vec3f v = vget(s, s->vel, s->vel_on, org[0] + i, org[1] + j, org[2] + k);
+            Vec3f dv = vget(s, s->vold, s->vold_on, org[0] + i, org[1] + j, org[2] + k);
+            for (int D = 0; D < 3; ++D) { vb[D * 1000 + o] = v.v[D]; db[D * 1000 + o] = dv.v[D]; }
+          }
+      for (size_t q = st[l]; q < st[l + 1]; ++q) {
+        const int* c = &s->cell[3 * q];
+        const int lc[3] = {c[0] - org[0], c[1] - org[1], c[2] - org[2]};
+        const float* p = &s->pos[3 * q];
+        float* pv = &s->vel_p[3 * q];
+        float* g = &s->gvel[3 * q];
+        for (int D = 0; D < 3; ++D) {
+          float v = interp_component(p, c, D, &vb[D * 1000], lc);
+          float dv = interp_component(p, c, D, &db[D * 1000], lc);
+          pv[D] = v + s->flip * ((dv + pv[D]) - v);
+          g[D] = v;
         }
-    for (size_t q = st[l]; q < st[l + 1]; ++q) {
-      const int* c = &s->cell[3 * q];
-      const int lc[3] = {c[0] - org[0], c[1] - org[1], c[2] - org[2]};
-      const float* p = &s->pos[3 * q];
-      float* pv = &s->vel_p[3 * q];
-      float* g = &s->gvel[3 * q];
-      for (int D = 0; D < 3; ++D) {
-        float v = interp_component(p, c, D, &vb[D * 1000], lc);
-        float dv = interp_component(p, c, D, &db[D * 1000], lc);
-        pv[D] = v + s->flip * ((dv + pv[D]) - v);
-        g[D] = v;
       }
     }
-  }
+  });
 }
 
 namespace {

@@ -3,7 +3,7 @@
  *
  * This library is the checker for the GPU implementation and the timed CPU
  * baseline.  Only tests/, __graft_entry__.smoke() and the CPU-baseline leg of
- * bench.py may load it.  It restates, single-threaded and with strict IEEE
+ * bench.py may load it.  It restates, with strict IEEE
  * float arithmetic (no FMA contraction, no fast-math), the single-partition
  * CPU path of schinmayee/fluid-sim-lb:
  *   common/flip_simulation.cc  (P2G, BCs, gravity, divergence, pressure
@@ -24,8 +24,11 @@
  * and it ships no tests or golden data, so this restatement is pinned by
  * known-answer tests only ("parity unpinned" against the reference binary).
  * OpenVDB's math::pcg internals (dot accumulation order/type, Jacobi apply)
- * are restated from their definitions: dots accumulate sequentially in T,
- * Jacobi is z = r * T(1.0/diag).
+ * are restated from their definitions: pcg::Vector::dot sums 100 contiguous
+ * chunks serially in T and adds the chunk totals in order (OpenVDB reduces
+ * contiguous ranges in parallel; the split is not pinned), the reference's
+ * own p.Ap loop is summed as the -Ofast build's 4-wide vector code would
+ * (four interleaved lanes, then the tail), and Jacobi is z = r * T(1.0/diag).
  */
 #ifndef FSIM_ORACLE_H
 #define FSIM_ORACLE_H
@@ -63,6 +66,13 @@ typedef struct orc_pcg_stats {
 orc_sim* orc_create(const int32_t dims[3], int32_t boundary, float gravity,
                     const float force[3], float flip, int32_t nppc);
 void orc_destroy(orc_sim* s);
+/* Host threads of the loops whose results do not depend on the thread count
+ * (per particle, per leaf, per matrix row or vector entry, the PCG dot
+ * products' chunk sums, whose totals are added in chunk order, and the four
+ * lane sums of p.Ap): every result is bit-identical for any n.
+ * Process-wide; 1 (the default) runs inline. */
+void orc_set_threads(int32_t n);
+int32_t orc_get_threads(void);
 void orc_add_solid_cuboid(orc_sim* s, const int32_t lo[3], const int32_t hi[3]);
 int32_t orc_is_solid(const orc_sim* s, int32_t i, int32_t j, int32_t k);
 

@@ -2,7 +2,9 @@
 
 The oracle (oracle/oracle.cc) restates the reference's single-partition CPU
 FLIP step.  It is the checker in tests/, in __graft_entry__.smoke() and the
-timed CPU baseline of bench.py; nothing else may load it.  Parity status:
+timed CPU baseline of bench.py; nothing else may load it.  It runs one host
+thread unless set_threads() says otherwise; its results do not depend on the
+thread count.  Parity status:
 unpinned against the reference binary (it cannot be built here); pinned by
 the known-answer tests in tests/test_oracle_kat.py.
 """
@@ -43,6 +45,8 @@ _SIGS = {
     "orc_create": (_P, [C.POINTER(C.c_int32), C.c_int32, C.c_float, C.POINTER(C.c_float),
                         C.c_float, C.c_int32]),
     "orc_destroy": (None, [_P]),
+    "orc_set_threads": (None, [C.c_int32]),
+    "orc_get_threads": (C.c_int32, []),
     "orc_add_solid_cuboid": (None, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "orc_is_solid": (C.c_int32, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "orc_seed": (C.c_int64, [_P, C.POINTER(orc_seed_pass), C.c_int32, C.c_uint64]),
@@ -289,6 +293,16 @@ class OracleSim:
     def set_marker(self, marker):
         marker = np.ascontiguousarray(marker, np.int32)
         self.lib.orc_set_marker(self.h, _ptr(marker))
+
+
+def set_threads(n: int) -> None:
+    """Host threads of the oracle's thread-count-independent loops (results
+    are bit-identical for any n); process-wide."""
+    load().orc_set_threads(int(n))
+
+
+def get_threads() -> int:
+    return int(load().orc_get_threads())
 
 
 def compute_dt(inv_speed, cfl, frame_step, time_in_frame):
