@@ -77,6 +77,8 @@ struct TopoRec {
   Buf<uint32_t> vel_on;  // n_gleaf*16, after the pressure update
   Buf<uint32_t> touched; // n_gleaf*16, faces P2G wrote (vold_on)
   Buf<uint32_t> normed;  // n_gleaf*16 words per component (x3): normalised faces
+  Buf<uint8_t> side;     // n_live: bit a set when the position after advection lies
+                         // below its cell's centre on axis a (the stencil side)
 };
 
 // Values of one step taped for the reverse stages; V = float (the fp32
@@ -111,6 +113,7 @@ struct TopoView {
   const uint32_t* vel_on;
   const uint32_t* touched;
   const uint32_t* normed;
+  const uint8_t* side;  // recorded stencil sides (new order), or null: from the position
   int n_pleaf, n_gleaf;
 };
 
@@ -149,19 +152,26 @@ __device__ __forceinline__ bool in_nodes(const int n[3], const int g[3]) {
 
 // Lower MAC node of component D for a particle binned in cell c (the rule of
 // ScatterWeight / InterpolateComponent, common/flip_simulation.cc:941-973)
-// and the offsets of the position from it.
+// and the offsets of the position from it.  The side of the cell centre on
+// each tangential axis is the recorded one (bit a of sb) when sb >= 0, so
+// the frozen map stays one polynomial piece around the recorded positions;
+// sb < 0 takes it from p.
 __device__ __forceinline__ void mac_stencil(int D, const int c[3], const double p[3], int st[3],
-                                            double fr[3]) {
+                                            double fr[3], int sb) {
 #pragma unroll
   for (int ax = 0; ax < 3; ++ax) {
     double lo = double(c[ax]);
     st[ax] = c[ax];
     if (ax != D) {
       lo += 0.5;
-      if (p[ax] < lo) { lo -= 1.0; st[ax] -= 1; }
+      const bool below = sb >= 0 ? ((sb >> ax) & 1) != 0 : p[ax] < lo;
+      if (below) { lo -= 1.0; st[ax] -= 1; }
     }
     fr[ax] = p[ax] - lo;
   }
+}
+__device__ __forceinline__ int side_of(const TopoView& t, int64_t i) {
+  return t.side ? int(t.side[i]) : -1;
 }
 // trilinear weight of corner (di,dj,dk) and its gradient in the position
 __device__ __forceinline__ double tri_w(const double f[3], int di, int dj, int dk, double g[3]) {
@@ -202,6 +212,22 @@ __global__ void k_count_diff(const uint32_t* __restrict__ a, const uint32_t* __r
   if (i < n && a[i] != b[i]) atomicAdd(cnt, 1ull);
 }
 
+// Stencil sides of the production step's positions after advection (new
+// order): float(c) + 0.5 is exact, so the fp32 comparison of ScatterWeight
+// and this one agree.
+__global__ void k_side_bits(const LeafMap lm, int64_t n, const uint32_t* __restrict__ keys,
+                            const float* __restrict__ x1, uint8_t* __restrict__ side) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int c[3];
+  key_cell(lm, keys[i], c);
+  int b = 0;
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax)
+    if (x1[ax * n + i] < float(c[ax]) + 0.5f) b |= 1 << ax;
+  side[i] = uint8_t(b);
+}
+
 // Normalised-face bits: P2G wrote the face and its weight sum passed the cut.
 __global__ void k_normed_bits(const TopoView t, const double* __restrict__ w,
                               uint32_t* __restrict__ out) {
@@ -228,7 +254,7 @@ __global__ void k_scatter(const TopoView t, int64_t n, const uint32_t* __restric
   for (int D = 0; D < 3; ++D) {
     int st[3];
     double fr[3];
-    mac_stencil(D, c, p, st, fr);
+    mac_stencil(D, c, p, st, fr, side_of(t, i));
     const double u = vp ? double(vp[D * n + i]) : 0.0;
     for (int q = 0; q < 8; ++q) {
       const int di = q >> 2, dj = (q >> 1) & 1, dk = q & 1;
@@ -394,7 +420,7 @@ __global__ void k_rp_g2p(const TopoView t, int64_t n, const uint32_t* __restrict
   for (int D = 0; D < 3; ++D) {
     int s3[3];
     double fr[3], gd[3];
-    mac_stencil(D, c, p, s3, fr);
+    mac_stencil(D, c, p, s3, fr, side_of(t, i));
     const double vi = interp(t, unew, t.vel_on, D, s3, fr, gd);
     const double di = interp(t, dv, t.touched, D, s3, fr, gd);
     st[D * n + i] = p[D];
@@ -462,7 +488,7 @@ __global__ void k_ad_g2p(const TopoView t, int64_t n, const uint32_t* __restrict
     vpb[D * n + i] = flip * vb[D * n + i];
     int st[3];
     double fr[3];
-    mac_stencil(D, c, p, st, fr);
+    mac_stencil(D, c, p, st, fr, side_of(t, i));
     for (int q = 0; q < 8; ++q) {
       const int di = q >> 2, dj = (q >> 1) & 1, dk = q & 1;
       const int g[3] = {st[0] + di, st[1] + dj, st[2] + dk};
@@ -596,7 +622,7 @@ __global__ void k_ad_p2g(const TopoView t, int64_t n, const uint32_t* __restrict
   for (int D = 0; D < 3; ++D) {
     int st[3];
     double fr[3];
-    mac_stencil(D, c, p, st, fr);
+    mac_stencil(D, c, p, st, fr, side_of(t, i));
     const double u = double(vp[D * n + i]);
     double acc = 0.0;
     for (int q = 0; q < 8; ++q) {
@@ -662,6 +688,9 @@ struct fsim_rollout {
   Buf<double> cell;                             // p-bar / divergence (cells)
   Buf<double> st64, st64b, m64, u64;            // replay state and grid scratch
   Buf<double> loss;
+  // PCG iterations of each step's replay solve, fixed by the first replay
+  // after a forward (0: not yet)
+  std::vector<int> replay_iters;
 };
 
 namespace {
@@ -692,6 +721,7 @@ TopoView view_of(fsim_rollout* r, const TopoRec* rec) {
   t.vel_on = s->vel_on;
   t.touched = s->vold_on;
   t.normed = rec ? rec->normed.p : nullptr;
+  t.side = rec ? rec->side.p : nullptr;
   t.n_pleaf = s->n_pleaf;
   t.n_gleaf = s->n_gleaf;
   return t;
@@ -822,6 +852,12 @@ int prod_step(fsim_rollout* r, int k, bool rec, Tape<float>* tp) {
     RB_CK(xs.reserve(size_t(3) * std::max<int64_t>(nl, 1)));
     FSIM_LAUNCH(s, "adj_pack_pos", k_pack3<float>, nblk(nl, 256), 256, 0, s->part[s->cur],
                 s->cap_p, nl, xs.p);
+    if (rec) {
+      RB_CK(T.side.reserve(size_t(std::max<int64_t>(nl, 1))));
+      FSIM_LAUNCH(s, "adj_side_bits", k_side_bits, nblk(nl, 256), 256, 0, s->lm, nl,
+                  s->keys[0], xs.p, T.side.p);
+    }
+    tv.side = T.side.p;  // recorded above, or by the recording pass of this step
     FSIM_LAUNCH(s, "adj_weights", k_scatter<float>, nblk(nl, 256), 256, 0, tv, nl, s->keys[0],
                 xs.p, static_cast<const float*>(nullptr), static_cast<double*>(nullptr), w);
     if (rec) {
@@ -915,11 +951,26 @@ int replay_step(fsim_rollout* r, int k, Tape<double>* tp, bool last_loss, double
               dt * double(s->cfg.force[0]), dt * double(s->cfg.force[1]),
               dt * double(s->cfg.force[2]), r->u64.p, V.vsave.p);
   FSIM_LAUNCH(s, "rp_divergence", k_rp_div, T.n_pleaf, 256, 0, tv, r->u64.p, r->cell.p);
+  // The first replay after a forward solves each step to relative residual
+  // 1e-12 and keeps the iteration count; later replays (the perturbed ones of
+  // finite differences) run exactly that many iterations.  CG with a fixed
+  // iteration count is a smooth function of its right-hand side, whereas a
+  // stopping test switches the count, and with it the result at the level of
+  // the solver's own error, between nearby right-hand sides.
   fsim_pcg_params p64 = solve64_params();
+  int& fixed_iters = r->replay_iters[size_t(k)];
+  if (fixed_iters > 0) {
+    p64.mode = FSIM_PCG_FIXED;
+    p64.max_iterations = fixed_iters;
+  }
   fsim_pcg_stats ps;
   std::memset(&ps, 0, sizeof(ps));
   if ((rc = pcg_solve(s, &p64, &ps, r->cell.p))) return rc;
   if (ps.status == FSIM_ERR_BREAKDOWN) return fail(s, FSIM_ERR_BREAKDOWN, "replay PCG breakdown");
+  if (fixed_iters <= 0) {
+    if (ps.status != FSIM_OK) return fail(s, ps.status, "replay PCG did not converge");
+    fixed_iters = std::max(ps.iterations, 1);
+  }
   FSIM_LAUNCH(s, "rp_pressure_update", k_rp_pupdate, T.n_gleaf, 256, 0, tv, r->u64.p,
               V.vsave.p, s->x64, V.unew.p, V.dv.p);
   FSIM_LAUNCH(s, "rp_g2p", k_rp_g2p, nblk(nl, 256), 256, 0, tv, nl, T.keys.p, V.x1.p, V.vp.p,
@@ -1137,6 +1188,7 @@ int fsim_rollout_forward(fsim_rollout_t* r, float dt, const fsim_pcg_params* pcg
   r->dt = dt;
   r->prm = *pcg;
   r->have_forward = false;
+  r->replay_iters.assign(size_t(r->steps), 0);
   const int64_t nt = int64_t(s->lm.n[0] + 2) * (s->lm.n[1] + 2) * (s->lm.n[2] + 2) * 3;
   RB_CK(r->target.reserve(size_t(nt)));
   RB_CK(cudaMemcpyAsync(r->target.p, target, size_t(nt) * sizeof(float), cudaMemcpyHostToDevice,

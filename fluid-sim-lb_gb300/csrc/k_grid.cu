@@ -241,6 +241,121 @@ __global__ void __launch_bounds__(256) k_p2g_cells(const __grid_constant__ GridA
   }
 }
 
+// Faces whose fixed-point weight sum is below kLowWeight are summed again
+// exactly as the reference sums them.  Fixed point has absolute resolution
+// (2^-33 per cell term), which is a relative error of up to 1e-4 in the
+// weight, and more in v = sum(w u) / sum(w), where the total weight is near
+// the 1e-5 normalisation cut; the reference's float sums are relative.  Such
+// faces are a few per thousand (the particles reaching them lie at the far
+// corner of their stencils), so the recompute costs little.
+constexpr float kLowWeight = 1e-3f;
+
+// The reference's float sums of component D at node g: ScatterWeight's
+// weights (common/flip_simulation.cc:976-990, differences of products) and
+// its order -- each particle leaf (in OpenVDB leaf order) sums its particles
+// in list order into its halo buffer (:853-868), and the buffers are added
+// into the grid leaf by leaf (:870-890).  Leaves of slot s's neighbourhood
+// only: a node of slot s is reached from cells within one cell of it.
+__device__ __noinline__ void ref_node_sums(const GridArgs& a, const int* nb, int s, int D,
+                                           const int g[3], float& tm, float& tw) {
+  int sl[3];
+  leaf_coords(a.lm, uint32_t(a.leaf_id[s]), sl[0], sl[1], sl[2]);
+  // cells that reach node g: c_D in {g_D - 1, g_D}, the others in g +- 1
+  int clo[3], chi[3], llo[3], lhi[3];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    clo[ax] = g[ax] - 1;
+    chi[ax] = ax == D ? g[ax] : g[ax] + 1;
+    llo[ax] = fdiv(clo[ax], 8);
+    lhi[ax] = fdiv(chi[ax], 8);
+  }
+  // candidate leaves in OpenVDB order (at most 8)
+  uint32_t lid[8];
+  int lslot[8], lc[8][3], nl = 0;
+  for (int lx = llo[0]; lx <= lhi[0]; ++lx)
+    for (int ly = llo[1]; ly <= lhi[1]; ++ly)
+      for (int lz = llo[2]; lz <= lhi[2]; ++lz) {
+        const int dx = lx - sl[0], dy = ly - sl[1], dz = lz - sl[2];
+        if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
+        const int ns = nb[nb_index(dx, dy, dz)];
+        if (ns < 0 || ns >= a.n_pleaf) continue;  // no particles there
+        const uint32_t id = uint32_t(a.leaf_id[ns]);
+        int q = nl++;
+        while (q > 0 && lid[q - 1] > id) {  // insertion sort by leaf id
+          lid[q] = lid[q - 1];
+          lslot[q] = lslot[q - 1];
+          lc[q][0] = lc[q - 1][0]; lc[q][1] = lc[q - 1][1]; lc[q][2] = lc[q - 1][2];
+          --q;
+        }
+        lid[q] = id;
+        lslot[q] = ns;
+        lc[q][0] = lx; lc[q][1] = ly; lc[q][2] = lz;
+      }
+  const float* px = a.part;
+  const int64_t cap = a.cap;
+  float Tm = 0.f, Tw = 0.f;
+  for (int l = 0; l < nl; ++l) {
+    float Bm = 0.f, Bw = 0.f;
+    bool touched = false;
+    const int x0 = max(clo[0], lc[l][0] * 8), x1 = min(chi[0], lc[l][0] * 8 + 7);
+    const int y0 = max(clo[1], lc[l][1] * 8), y1 = min(chi[1], lc[l][1] * 8 + 7);
+    const int z0 = max(clo[2], lc[l][2] * 8), z1 = min(chi[2], lc[l][2] * 8 + 7);
+    for (int cx = x0; cx <= x1; ++cx)
+      for (int cy = y0; cy <= y1; ++cy)
+        for (int cz = z0; cz <= z1; ++cz) {
+          const int v = ((cx & 7) << 6) | ((cy & 7) << 3) | (cz & 7);
+          const uint2 rg = a.cell_range[int64_t(lslot[l]) * 512 + v];
+          const int c[3] = {cx, cy, cz};
+          for (uint32_t q = rg.x; q < rg.y; ++q) {
+            if (a.check_dead && a.keys[q] == kDeadKey) continue;
+            float f[3];
+            int corner[3];
+            bool reach = true;
+#pragma unroll
+            for (int ax = 0; ax < 3; ++ax) {
+              const float pa = px[ax * cap + q];
+              float lo = float(c[ax]);
+              int st = c[ax];
+              if (ax != D) {
+                lo = __fadd_rn(lo, 0.5f);
+                if (pa < lo) { lo = __fsub_rn(lo, 1.0f); st -= 1; }
+              }
+              f[ax] = __fsub_rn(pa, lo);
+              corner[ax] = g[ax] - st;
+              reach = reach && (corner[ax] == 0 || corner[ax] == 1);
+            }
+            if (!reach) continue;
+            touched = true;
+            const float x = f[0], y = f[1], z = f[2];
+            const float xy = __fmul_rn(x, y), yz = __fmul_rn(y, z), xz = __fmul_rn(z, x);
+            const float xyz = __fmul_rn(xy, z);
+            const float w110 = __fsub_rn(xy, xyz), w101 = __fsub_rn(xz, xyz);
+            const float w001 = __fsub_rn(__fsub_rn(z, yz), w101);
+            const int k = (corner[0] << 2) | (corner[1] << 1) | corner[2];
+            float w;
+            switch (k) {
+              case 7: w = xyz; break;
+              case 6: w = w110; break;
+              case 5: w = w101; break;
+              case 4: w = __fsub_rn(__fsub_rn(x, xz), w110); break;
+              case 3: w = __fsub_rn(yz, xyz); break;
+              case 2: w = __fsub_rn(__fsub_rn(y, yz), w110); break;
+              case 1: w = w001; break;
+              default: w = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(1.0f, x), y), xy), w001);
+            }
+            Bm = __fadd_rn(Bm, __fmul_rn(w, px[(3 + D) * cap + q]));
+            Bw = __fadd_rn(Bw, w);
+          }
+        }
+    if (touched) {
+      Tm = __fadd_rn(Tm, Bm);
+      Tw = __fadd_rn(Tw, Bw);
+    }
+  }
+  tm = Tm;
+  tw = Tw;
+}
+
 template <bool FUSED>
 __global__ void __launch_bounds__(256) k_p2g_nodes(const __grid_constant__ GridArgs a) {
   __shared__ int nb[27];
@@ -302,11 +417,13 @@ __global__ void __launch_bounds__(256) k_p2g_nodes(const __grid_constant__ GridA
     float wsum[3];
 #pragma unroll
     for (int D = 0; D < 3; ++D) {
-      const float ws = from_fix(sw[D]);
+      float ws = from_fix(sw[D]);
+      float ms = from_fix(sv[D]);
+      if (on && ws < kLowWeight) ref_node_sums(a, nb, s, D, g, ms, ws);
       wsum[D] = ws;
       // THRESH is a double literal in the reference: float ws < 1e-5 (double)
       // is ws <= 1e-5f
-      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(from_fix(sv[D]), ws)) : 0.f;
+      val[D] = on ? ((ws <= 1e-5f) ? 0.f : __fdiv_rn(ms, ws)) : 0.f;
     }
     // marker: FLUID for in-box cells holding particles
     bool has = false;

@@ -415,7 +415,9 @@ int fsim_particles_to_level_set(fsim_t* sim, float radius, float half_width,
  *
  * Gradients are those of the rollout with the discrete choices frozen at the
  * forward run: particle binning and sort order, wall clamping and deletion,
- * FLUID markers, active faces and the 1e-5 weight cut.  The pressure solves
+ * the side of the cell centre each particle's trilinear stencil starts on
+ * (ScatterWeight / InterpolateComponent), FLUID markers, active faces and
+ * the 1e-5 weight cut.  The pressure solves
  * are taken as exact (A is symmetric, so the adjoint solve is the same PCG).
  * The forward keeps a checkpoint of the particle state every
  * checkpoint_every steps and the frozen topology of every step; the backward
@@ -448,7 +450,10 @@ int fsim_rollout_backward(fsim_rollout_t* r, int32_t tape, const fsim_pcg_params
                           double* grad_vel, double* grad_gvel);
 /* Loss of an fp64 replay of the forward with the frozen topology from the
  * initial positions and the given initial vel / gvel (null: the stored
- * ones); pressure solves in FP64 to relative residual 1e-12. */
+ * ones).  Pressure solves in FP64: the first replay after a forward solves
+ * each step to relative residual 1e-12 and keeps its iteration count, and
+ * every later replay runs exactly those counts, so the replay loss is a
+ * smooth function of vel / gvel (what central differences need). */
 int fsim_rollout_replay_loss(fsim_rollout_t* r, const double* vel, const double* gvel,
                              double* loss);
 
