@@ -322,6 +322,7 @@ int fsim_destroy(fsim_t* s) {
   dfree(s->io_stage);
   if (s->p2g_nodes) cudaFree(s->p2g_nodes);
   if (s->p2g_touch) cudaFree(s->p2g_touch);
+  if (s->p2g_low) cudaFree(s->p2g_low);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return FSIM_OK;

@@ -187,6 +187,8 @@ struct fsim_sim {
   // P2G pass 1 output (k_grid.cu): per particle leaf the 10^3 node block
   unsigned long long* p2g_nodes = nullptr;
   uint32_t* p2g_touch = nullptr;
+  uint32_t* p2g_low = nullptr;  // [0] count, then the low-weight faces of P2G pass 2
+  int64_t p2g_low_cap = 0;
   int64_t p2g_cap = 0;
   // fsim_step_host: a second stream for the copies that overlap the step
   cudaStream_t io_stream = nullptr;

@@ -49,6 +49,8 @@ struct GridArgs {
   int64_t* cnt;
   unsigned long long* p2g_nodes;  // P2G pass 1 output: [particle leaf][6][1000]
   uint32_t* p2g_touch;            // [particle leaf][32] touched bits of the 1000 nodes
+  uint32_t* p2g_low;              // [0]: count; then slot * 1536 + D * 512 + voxel of the
+                                  // low-weight faces pass 2 leaves to k_p2g_low
 };
 
 __device__ __forceinline__ void origin_of(const GridArgs& a, int s, int o[3]) {
@@ -245,9 +247,9 @@ __global__ void __launch_bounds__(256) k_p2g_cells(const __grid_constant__ GridA
 // exactly as the reference sums them.  Fixed point has absolute resolution
 // (2^-33 per cell term), which is a relative error of up to 1e-4 in the
 // weight, and more in v = sum(w u) / sum(w), where the total weight is near
-// the 1e-5 normalisation cut; the reference's float sums are relative.  Such
-// faces are a few per thousand (the particles reaching them lie at the far
-// corner of their stencils), so the recompute costs little.
+// the 1e-5 normalisation cut; the reference's float sums are relative.  Pass
+// 2 lists those faces and k_p2g_low re-sums them, one thread per face, so
+// pass 2 keeps its registers and occupancy.
 constexpr float kLowWeight = 1e-3f;
 
 // The reference's float sums of component D at node g: ScatterWeight's
@@ -417,9 +419,10 @@ __global__ void __launch_bounds__(256) k_p2g_nodes(const __grid_constant__ GridA
     float wsum[3];
 #pragma unroll
     for (int D = 0; D < 3; ++D) {
-      float ws = from_fix(sw[D]);
-      float ms = from_fix(sv[D]);
-      if (on && ws < kLowWeight) ref_node_sums(a, nb, s, D, g, ms, ws);
+      const float ws = from_fix(sw[D]);
+      const float ms = from_fix(sv[D]);
+      if (on && ws < kLowWeight)  // re-summed by k_p2g_low, which rewrites this face
+        a.p2g_low[1 + atomicAdd(a.p2g_low, 1u)] = unsigned(s) * 1536u + unsigned(D * 512 + v);
       wsum[D] = ws;
       // THRESH is a double literal in the reference: float ws < 1e-5 (double)
       // is ws <= 1e-5f
@@ -466,6 +469,38 @@ __global__ void __launch_bounds__(256) k_p2g_nodes(const __grid_constant__ GridA
     }
     if ((threadIdx.x & 31) == 0) a.vel_on[int64_t(s) * 16 + (v >> 5)] = ball;
     a.marker[int64_t(s) * 512 + v] = int8_t(m);
+  }
+}
+
+// The low-weight faces pass 2 listed: the reference's float sums
+// (ref_node_sums), normalisation with the 1e-5 cut, and for the fused step
+// the rest of pass 2's per-face work (BC, SaveGridVelocities, AddGravity,
+// BC).  The faces are independent, so the list's order does not matter.
+template <bool FUSED>
+__global__ void __launch_bounds__(128) k_p2g_low(const __grid_constant__ GridArgs a) {
+  const unsigned n = *a.p2g_low;
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const unsigned code = a.p2g_low[1 + e];
+    const int s = int(code / 1536u), D = int((code % 1536u) >> 9), v = int(code & 511u);
+    int org[3];
+    origin_of(a, s, org);
+    const int g[3] = {org[0] + (v >> 6), org[1] + ((v >> 3) & 7), org[2] + (v & 7)};
+    float ms, ws;
+    ref_node_sums(a, a.nbr + int64_t(s) * 27, s, D, g, ms, ws);
+    const float val = (ws <= 1e-5f) ? 0.f : __fdiv_rn(ms, ws);
+    const int64_t o = int64_t(s) * 1536 + D * 512 + v;
+    if (FUSED) {
+      const bool sc = is_solid(a.sd, g[0], g[1], g[2]);
+      const bool zero = sc != is_solid(a.sd, g[0] - (D == 0), g[1] - (D == 1), g[2] - (D == 2));
+      const float gf = __fmul_rn(a.dt, D == 0 ? a.fx : (D == 1 ? a.fy : a.fz));
+      float vv = zero ? 0.f : val;                              // ApplyBoundaryConditions
+      a.vold[o] = vv;                                           // SaveGridVelocities
+      vv = (D == 1) ? __fsub_rn(vv, gf) : __fadd_rn(vv, gf);    // AddGravity
+      a.vel[o] = zero ? 0.f : vv;                               // ApplyBoundaryConditions
+    } else {
+      a.vel[o] = val;
+      a.weight[o] = ws;
+    }
   }
 }
 
@@ -818,13 +853,31 @@ int launch_p2g(fsim_sim* s, bool fused, float dt) {
     FSIM_CK(s, cudaMalloc(&s->p2g_touch, size_t(s->cap_pleaf) * 32 * 4));
     s->p2g_cap = s->cap_pleaf;
   }
+  // list of low-weight faces: at most every face of every grid leaf, each
+  // coded in 32 bits as slot * 1536 + D * 512 + voxel
+  if (int64_t(s->n_gleaf) * 1536 >= (int64_t(1) << 32))
+    return fail(s, FSIM_ERR_CAPACITY, "too many grid leaves for the P2G low-weight face list");
+  const int64_t low_cap = int64_t(s->cap_leaf) * 1536 + 1;
+  if (s->p2g_low_cap < low_cap) {
+    if (s->p2g_low) cudaFree(s->p2g_low);
+    s->p2g_low = nullptr;
+    s->p2g_low_cap = 0;
+    FSIM_CK(s, cudaMalloc(&s->p2g_low, size_t(low_cap) * sizeof(uint32_t)));
+    s->p2g_low_cap = low_cap;
+  }
   GridArgs a = make_args(s);
   a.dt = dt;
+  a.p2g_low = s->p2g_low;
+  FSIM_CK(s, cudaMemsetAsync(s->p2g_low, 0, sizeof(uint32_t), s->stream));
   FSIM_LAUNCH(s, fused ? "p2g_cells_fused" : "p2g_cells", k_p2g_cells, s->n_pleaf, 256, 0, a);
-  if (fused)
+  const int lgrid = std::max(1, s->num_sms * 4);
+  if (fused) {
     FSIM_LAUNCH(s, "p2g_fused", k_p2g_nodes<true>, s->n_gleaf, 256, 0, a);
-  else
+    FSIM_LAUNCH(s, "p2g_low_fused", k_p2g_low<true>, lgrid, 128, 0, a);
+  } else {
     FSIM_LAUNCH(s, "p2g", k_p2g_nodes<false>, s->n_gleaf, 256, 0, a);
+    FSIM_LAUNCH(s, "p2g_low", k_p2g_low<false>, lgrid, 128, 0, a);
+  }
   return FSIM_OK;
 }
 
