@@ -46,6 +46,11 @@ def test_gpu_tank_case_against_fixture():
     pos, vel, gvel = sim.download_particles()
     assert pos.shape == ref["pos"].shape
     assert rel_l2(pos, ref["pos"]) <= 1e-6
+    # The GPU's fp32 solves stop at relative residual 1e-5 after other iteration counts
+    # than the fixture's (different dot-product summation orders), so each differs from
+    # the converged solve by the solver's own error; two such solves differ by up to the
+    # sum of the two (tests/test_gpu_configs.py measures both errors).  1e-4 bounds that
+    # sum here; bitwise topology is asserted above.
     assert rel_l2(vel, ref["vel"]) <= 1e-4
     p, pa = sim.field(fsim.FIELD_PRESSURE)
     assert np.array_equal(pa, ref["pressure_active"])
