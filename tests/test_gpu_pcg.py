@@ -97,9 +97,9 @@ def test_reference_absolute_rule():
     assert abs(st.iterations - ost.iterations) <= 2
     assert st.rr < prm.threshold
     a, b = _pressures(sim, orc)
-    # both stop at the reference's absolute threshold on r.r (loose: sqrt(rr/bb) ~ 3e-5 here)
-    # after iteration counts up to 2 apart, so they differ by that solver error, not by
-    # the kernels (the fixed-iteration test above holds 1e-5)
+    # both stop at the reference's absolute threshold on r.r after iteration counts up to
+    # 2 apart, so they differ by that solver's own error, not by the kernels (the
+    # fixed-iteration test above holds 1e-5)
     assert rel_l2(a, b) <= 1e-4
     sim.close()
 
