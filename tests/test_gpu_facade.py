@@ -84,3 +84,65 @@ def test_debug_dumps_use_the_reference_text_format(tmp_path):
     lines = (d / "particles_00000000").read_text().splitlines()
     n = int(lines[2])
     assert len(lines) == 3 + n and lines[3].startswith("0 : ")
+
+
+def test_written_values_match_the_state(tmp_path):
+    """The writers' values, not only their layout: the demo's fused run of a
+    32^3 sphere drop (3 steps, the reference's default solver) is repeated
+    through the C ABI in this process (the step is bitwise reproducible), and
+    the binary frame (common/particles.cc:185-198) must hold the downloaded
+    positions and velocities bit for bit, in order; the text dumps
+    (Particles / VectorGrid / ScalarGrid::Write, "%f") must hold them to the
+    printed precision, on exactly the active voxels."""
+    import fsim
+
+    if not DEMO.exists():
+        pytest.skip("fsim_demo not built")
+    n, steps = 32, 3
+    out = tmp_path / "w"
+    r = subprocess.run([str(DEMO), str(n), str(steps), str(out), "fused", "debug"],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    g, f = fsim.physical_gravity(n)
+    sim = fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f, 0.95, 8)
+    sim.seed(fsim.scene_passes("sphere_drop", n), seed=0)
+    prm = sim.default_pcg_params()
+    frame_step = float(np.float32(1.0) / np.float32(30.0))
+    inv, t = sim.cfl(), 0.0
+    for _ in range(steps):
+        dt, t = fsim.compute_dt(inv, 1, frame_step, t)
+        if np.float32(t) + np.float32(1e-5) >= np.float32(frame_step):
+            t = 0.0
+        inv = sim.step(dt, prm).next_inv_speed
+    pos, vel, _ = sim.download_particles()
+    u, ua = sim.field(fsim.FIELD_VELOCITY)
+    p, pa = sim.field(fsim.FIELD_PRESSURE)
+    sim.close()
+    part = Path(str(out) + "_0")
+    data = (part / "particles_00000000").read_bytes()
+    cnt = struct.unpack("7i", data[:28])[6]
+    assert cnt == pos.shape[0]
+    rec = np.frombuffer(data[28:], dtype=np.dtype([("id", "<i4"), ("p", "<f4", 3),
+                                                   ("v", "<f4", 3)]))
+    assert np.array_equal(rec["p"], pos) and np.array_equal(rec["v"], vel)
+    half_ulp = 5.0e-7 + 1e-12  # "%f" prints six decimals
+    lines = (part / "debug" / "particles_00000000").read_text().splitlines()
+    txt = np.array([[float(x) for x in re.split(r"[ ,:]+", ln.strip())[1:]] for ln in lines[3:]])
+    assert txt.shape == (cnt, 6)
+    assert np.abs(txt[:, :3] - pos).max() <= half_ulp
+    assert np.abs(txt[:, 3:] - vel).max() <= half_ulp
+    # the velocity dump covers the faces of [0, N]^3, the pressure dump the cells of [0, N)^3
+    for name, field, act, nval, hi in (("grid_velocity_00000000.txt", u, ua, 3, n),
+                                       ("grid_phi_00000000.txt", p, pa, 1, n - 1)):
+        rows = (part / "debug" / name).read_text().splitlines()[2:]
+        got = {}
+        for ln in rows:
+            ijk, vals = ln.split(" : ")
+            got[tuple(int(x) for x in ijk.split())] = [float(x) for x in vals.split()]
+        active = {tuple(int(x) - 1 for x in c) for c in np.argwhere(act)}
+        assert len(got) > 0
+        assert set(got) == {c for c in active if all(0 <= x <= hi for x in c)}, name
+        for c, vals in got.items():
+            ref = np.atleast_1d(field[c[0] + 1, c[1] + 1, c[2] + 1]).astype(np.float64)
+            assert len(vals) == nval
+            assert np.abs(np.array(vals) - ref).max() <= half_ulp, (name, c)

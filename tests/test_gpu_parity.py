@@ -309,6 +309,44 @@ def test_step_deterministic():
     assert rel_l2(outs[0][3], outs[1][3]) <= FIELD_RTOL
 
 
+def test_run_frames_against_oracle():
+    """fsim_run_frames (the frames x While(dt) loop of the reference driver,
+    common/flip_app_sim.cc:357-462) against the oracle's dt rule
+    (orc_compute_dt) and RunOneStep (orc_step), both with converged solves
+    (GPU MIXED to 1e-10, oracle FP64 to 1e-13) so that the free-running
+    trajectories stay within the field bar: the same number of steps per
+    frame, the same time, and the final state within 1e-5 (positions and
+    velocities; binning and leaves exactly)."""
+    from oracle.oracle import compute_dt
+
+    n = 24
+    orc = make_oracle(n, "sphere_drop", noise=_noise(n))
+    sim = make_gpu(orc)
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 2000, tolerance=1e-10,
+                          inner_tolerance=1e-4)
+    st = sim.run_frames(2, prm, frame_rate=30.0)
+    frame_step = float(np.float32(1.0) / np.float32(30.0))
+    inv, steps, dts = orc.cfl(), 0, []
+    for _ in range(2):
+        t = 0.0
+        while t + 1e-5 < frame_step:
+            dt, t = compute_dt(inv, 1, frame_step, t)
+            orc.step(dt, mode=1, precision=2, max_iterations=20000, tol=1e-13)
+            inv = orc.cfl()
+            dts.append(dt)
+            steps += 1
+    assert st.frames == 2 and st.steps == steps, (st.steps, steps)
+    assert abs(st.last_dt - dts[-1]) <= 1e-5 * dts[-1]
+    assert abs(st.time - orc.time) <= 1e-6 * orc.time
+    p1, v1, g1 = sim.download_particles()
+    p0, v0, g0 = orc.particles()
+    assert p1.shape == p0.shape
+    assert np.array_equal(sim.leaves(), orc.leaves())
+    assert rel_l2(p1, p0) <= FIELD_RTOL
+    assert rel_l2(v1, v0) <= FIELD_RTOL and rel_l2(g1, g0) <= FIELD_RTOL
+    sim.close()
+
+
 def test_run_frames_equals_stepping_by_hand():
     """fsim_run_frames is the driver's frame loop: the same dt sequence and
     state as fsim_compute_dt + fsim_step called by hand."""
