@@ -252,6 +252,11 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if (const char* c = std::getenv("FSIM_PCG_PDL")) s->use_pdl = c[0] != '0';
   // FSIM_PCG_ZDIRECT=0/1: z-face planes or direct reads (default: by system size)
   if (const char* c = std::getenv("FSIM_PCG_ZDIRECT")) s->zdirect = c[0] == '1' ? 1 : 0;
+  // FSIM_PCG_TMA=1: the bulk-copy staged spmv (opt-in)
+  if (const char* c = std::getenv("FSIM_PCG_TMA")) s->tma_spmv = c[0] == '1' ? 1 : 0;
+  // FSIM_PCG_TMA_WITHHOLD=1 (tests): the first solve's bulk-copy spmv holds one
+  // stage's flags copy back until its wait has given up
+  if (const char* c = std::getenv("FSIM_PCG_TMA_WITHHOLD")) s->tma_withhold = c[0] == '1';
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels
   if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
   for (int a = 0; a < 3; ++a) {

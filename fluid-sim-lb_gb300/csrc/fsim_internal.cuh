@@ -159,6 +159,8 @@ struct alignas(16) PcgScalars {
   double tol2_outer;  // MIXED: outer tolerance squared; a segment never stops below tol2_outer*bb
   unsigned int cnt_s, cnt_r;
   unsigned long long n_rows;  // FLUID cells (unknowns), counted by setup
+  // bulk-copy spmv: FSIM_ERR_TIMEOUT when a bounded stage wait gave up (0: none)
+  unsigned int wait_err, wait_pad[3];
   // hot-loop hand-off: [0] spmv -> update, [1] update -> spmv (and setup /
   // residual replacement -> spmv)
   PcgIterState st[2];
@@ -295,6 +297,11 @@ struct fsim_sim {
   // z-face neighbours of the pipelined kernels: -1 by system size, 0 planes,
   // 1 direct reads (FSIM_PCG_ZDIRECT)
   int zdirect = -1;
+  // bulk-copy staged spmv (FSIM_PCG_TMA=1; measured slower, opt-in); tests
+  // only: the next solve withholds one stage's flags copy until the stage's
+  // bounded wait has given up (FSIM_PCG_TMA_WITHHOLD=1)
+  int tma_spmv = 0;
+  int tma_withhold = 0;
   // register-pipelined hot kernels (next half leaf loaded during the
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;

@@ -301,6 +301,7 @@ struct PcgArgs {
   float* partf;     // fp32 / double-float block partials of the hot kernels (FP32, MIXED)
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
   int par;          // spmv / update: parity of the iteration this launch serves
+  int withhold;     // bulk-copy spmv, test only: CTA 0's first stage withholds its flags copy
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
 };
 
@@ -1225,6 +1226,232 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_pl(const __grid_con
   put_partials<DM, 1>(a, kPartPAp, v);
 }
 
+
+// ---- bulk-copy (TMA) staged spmv for large systems --------------------------------
+// A half leaf's own r, p_{j-1} and flags are 1 KB + 1 KB + 256 B, contiguous.
+// Lane 0 of each warp copies them into a ring of kStages shared-memory stages
+// with cp.async.bulk (the SM's copy engine: no registers, no load/store-unit
+// slots), kStages - 1 half leaves ahead; an mbarrier per stage counts the
+// bytes in.  The halo column and the z faces (32 B and 4 B per lane,
+// scattered) are loaded into registers one half leaf ahead, as in
+// k_pcg_spmv_pl.  The ring keeps twice the register kernel's own-column
+// bytes in flight per warp, but it measured slower at every size (spmv per
+// launch: 25.4 vs 21.4 us at 256^3, 83 vs 65 us at 512^3, 480 vs 350 us at
+// 1024^3): the ring's shared memory leaves the SM little L1 for the halo
+// and z-face loads, and the stage adds a shared-memory round trip.  It is
+// opt-in (FSIM_PCG_TMA=1) and gives bit-identical solves.
+//
+// Every wait is bounded (kStagePolls).  A wait that gives up records
+// FSIM_ERR_TIMEOUT in PcgScalars::wait_err, issues the stage's withheld copy
+// if there is one, and waits again with a long bound, so that no copy is in
+// flight into shared memory when the CTA exits.  PcgArgs::withhold (tests
+// only) makes CTA 0's first stage hold back its flags copy, and that stage's
+// wait gives up after kHeldPolls: the wait runs out without a fault, and the
+// solve still completes with the right values.
+constexpr int kStages = 4;
+constexpr unsigned kStagePolls = 1u << 22;  // bound of a stage wait
+constexpr unsigned kHeldPolls = 256;        // the test's withheld stage (it cannot fill)
+constexpr unsigned kDrainPolls = 1u << 26;  // second, long bound after a wait gave up
+
+struct SpmvStage {
+  float r[256];
+  float p[256];
+  uint8_t f[256];
+};
+// the stage ring is dynamic shared memory (above the 48 KB static limit with
+// the kernel's static tiles and head stage)
+constexpr size_t kTmaDynSmem = size_t(kHotThreads / 32) * kStages * sizeof(SpmvStage);
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, unsigned parity, unsigned polls) {
+  for (unsigned i = 0; i < polls; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+// Lane 0: copy half leaf hw's own columns into stage st (the flags copy held
+// back when `hold`).
+__device__ __forceinline__ void spmv_stage_issue(const PcgArgs& a, int hw, const float* r,
+                                                 const float* pold, SpmvStage& st,
+                                                 uint64_t* bar, bool hold) {
+  const int64_t o = int64_t(hw >> 1) * 512 + (hw & 1) * 256;
+  mbar_expect_tx(bar, 2u * 1024u + 256u);
+  bulk_g2s(st.r, r + o, 1024u, bar);
+  bulk_g2s(st.p, pold + o, 1024u, bar);
+  if (!hold) bulk_g2s(st.f, a.flags + o, 256u, bar);
+}
+
+// Lane 0: the bounded wait on stage q (phase parity ph), with the recovery
+// above; the warp learns the outcome by a shuffle.
+// held: this stage's flags copy was withheld (the test's first stage only).
+__device__ __forceinline__ void stage_wait(const PcgArgs& a, int lane, uint64_t* bar,
+                                           unsigned ph, bool* held, int hw, SpmvStage& st) {
+  const unsigned polls = (held && *held) ? kHeldPolls : kStagePolls;
+  if (lane == 0 && !mbar_wait_n(bar, ph, polls)) {
+    atomicExch(&a.sc->wait_err, unsigned(FSIM_ERR_TIMEOUT));
+    if (held && *held) {  // the test's withheld copy: complete the stage now
+      const int64_t o = int64_t(hw >> 1) * 512 + (hw & 1) * 256;
+      bulk_g2s(st.f, a.flags + o, 256u, bar);
+      *held = false;
+    }
+    if (!mbar_wait_n(bar, ph, kDrainPolls)) atomicExch(&a.sc->wait_err, unsigned(FSIM_ERR_CUDA));
+  }
+  __syncwarp();
+}
+
+template <int DM, bool ZD>
+__global__ void __launch_bounds__(kHotThreads, 4) k_pcg_spmv_tma(const __grid_constant__ PcgArgs a) {
+  pdl_wait();  // reads its predecessor's r from the first copy on
+  pdl_trigger();
+  using T = float;
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<2, PartT<DM>> hs;
+  extern __shared__ __align__(128) unsigned char tma_ring[];  // kTmaDynSmem bytes
+  __shared__ __align__(8) uint64_t bars[kHotThreads / 32][kStages];
+  const int par = a.par;
+  const T* r = static_cast<const T*>(a.r);
+  const T* pold = static_cast<const T*>(par ? a.p0 : a.p1);
+  T* pnew = static_cast<T*>(par ? a.p1 : a.p0);
+  const int qold = 1 + (par ^ 1), qnew = 1 + par;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  const int hw0 = blockIdx.x * wpb + w;
+  SpmvStage* stg = reinterpret_cast<SpmvStage*>(tma_ring) + w * kStages;
+  uint64_t* bar = bars[w];
+  bool held = a.withhold && blockIdx.x == 0 && w == 0 && hw0 < nhw;  // lane 0's copy only
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < kStages; ++q) mbar_init(&bar[q], 1u);
+    fence_async_smem();
+  }
+  __syncwarp();
+  if (lane == 0) {
+    for (int q = 0; q < kStages - 1; ++q) {
+      const int hq = hw0 + q * hstride;
+      if (hq < nhw) spmv_stage_issue(a, hq, r, pold, stg[q], &bar[q], held && q == 0);
+    }
+  }
+  head_issue<DM, 2>(hs, a, 0);
+  fill_diag_table<T>(tab);
+  SpmvIn<T> cur;  // halo and z faces only (rc, pc, f come from the stage)
+  int nbl = -1;
+  if (hw0 < nhw) {
+    int fs[6];
+    face_slots(face_slot_lane(a.nbr, hw0 >> 1, lane), fs);
+    nbl = hw0 + hstride < nhw ? face_slot_lane(a.nbr, (hw0 + hstride) >> 1, lane) : -1;
+    spmv_load_halo<T, ZD>(a, hw0, lane, fs, r, pold, qold, cur);
+  }
+  const HotHead head = spmv_head<DM>(hs, a);
+  if (head.done) {
+    // no work: drain the copies already issued before leaving
+    for (int q = 0; q < kStages - 1; ++q)
+      if (hw0 + q * hstride < nhw)
+        stage_wait(a, lane, &bar[q], 0u, q == 0 ? &held : nullptr, hw0 + q * hstride, stg[q]);
+    return;
+  }
+  const T beta = T(head.s);
+  Tile<T>& tile = tiles[w];
+  Dot<DM> dp;
+  int k = 0;
+  for (int hw = hw0; hw < nhw; hw += hstride, ++k) {
+    // keep kStages - 1 half leaves in flight: refill the stage read last time
+    {
+      const int hq = hw + (kStages - 1) * hstride;
+      const int q = (k + kStages - 1) % kStages;
+      if (lane == 0 && hq < nhw) spmv_stage_issue(a, hq, r, pold, stg[q], &bar[q], false);
+    }
+    const int hn = hw + hstride;
+    SpmvIn<T> nxt;
+    if (hn < nhw) {
+      int fs[6];
+      face_slots(nbl, fs);
+      spmv_load_halo<T, ZD>(a, hn, lane, fs, r, pold, qold, nxt);
+      nbl = hn + hstride < nhw ? face_slot_lane(a.nbr, (hn + hstride) >> 1, lane) : -1;
+    }
+    const int q = k % kStages;
+    stage_wait(a, lane, &bar[q], unsigned((k / kStages) & 1), k == 0 ? &held : nullptr, hw,
+               stg[q]);
+    const HalfLeaf h = half_pos(hw, lane);
+    {
+      const float4 a0 = reinterpret_cast<const float4*>(stg[q].r)[2 * lane];
+      const float4 a1 = reinterpret_cast<const float4*>(stg[q].r)[2 * lane + 1];
+      const float4 b0 = reinterpret_cast<const float4*>(stg[q].p)[2 * lane];
+      const float4 b1 = reinterpret_cast<const float4*>(stg[q].p)[2 * lane + 1];
+      cur.f = reinterpret_cast<const uint2*>(stg[q].f)[lane];
+      cur.rc.v[0] = a0.x; cur.rc.v[1] = a0.y; cur.rc.v[2] = a0.z; cur.rc.v[3] = a0.w;
+      cur.rc.v[4] = a1.x; cur.rc.v[5] = a1.y; cur.rc.v[6] = a1.z; cur.rc.v[7] = a1.w;
+      cur.pc.v[0] = b0.x; cur.pc.v[1] = b0.y; cur.pc.v[2] = b0.z; cur.pc.v[3] = b0.w;
+      cur.pc.v[4] = b1.x; cur.pc.v[5] = b1.y; cur.pc.v[6] = b1.z; cur.pc.v[7] = b1.w;
+    }
+    __syncwarp();
+    if (lane == 0) fence_async_smem();  // this stage's reads before its next bulk write
+    Col<T> P, H;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      P.v[z] = pnew_of<T>(tab, fbyte(cur.f, z), cur.rc.v[z], cur.pc.v[z], beta);
+      H.v[z] = pnew_of<T>(tab, fbyte(cur.hf, z), cur.hr.v[z], cur.hp.v[z], beta);
+    }
+    const T zm = pnew_of<T>(tab, cur.zf0, cur.zr0, cur.zq0, beta);
+    const T zp = pnew_of<T>(tab, cur.zf1, cur.zr1, cur.zq1, beta);
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
+    stcol(pnew, o, P);
+    if constexpr (!ZD) {  // publish the z faces for the neighbours
+      T* zw = static_cast<T*>(a.zf) + (unsigned(h.s) * 384u + 128u * unsigned(qnew) + unsigned(h.fidx));
+      zw[0] = P.v[0];
+      zw[64] = P.v[7];
+    }
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, cur.f, zm, zp, ap);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
+    cur.hf = nxt.hf;
+    cur.hr = nxt.hr;
+    cur.hp = nxt.hp;
+    cur.zf0 = nxt.zf0; cur.zf1 = nxt.zf1;
+    cur.zr0 = nxt.zr0; cur.zr1 = nxt.zr1;
+    cur.zq0 = nxt.zq0; cur.zq1 = nxt.zq1;
+  }
+  PartT<DM> v[1] = {dp.pvalue()};
+  put_partials<DM, 1>(a, kPartPAp, v);
+}
+
 template <typename T>
 struct UpdIn {
   uint2 f;
@@ -1454,16 +1681,36 @@ __global__ void k_to_pressure(const T* __restrict__ x, float* __restrict__ pres,
     pres[o] = float(x[o]);
 }
 
+// The spmv whose own columns are staged by bulk copies (k_pcg_spmv_tma):
+// opt-in, FSIM_PCG_TMA=1.
+template <typename T>
+bool use_tma_spmv(const fsim_sim* s, int /*n_pleaf*/) {
+  return std::is_same<T, float>::value && s->use_pipe && s->tma_spmv;
+}
+
 // The hot kernel pair of a solve: the register-pipelined pair (fp32
-// vectors), or the plain pair (fp64 vectors, or FSIM_PCG_PIPE=0).
+// vectors; FSIM_PCG_TMA=1: the bulk-copy staged spmv), or the plain pair
+// (fp64 vectors, or FSIM_PCG_PIPE=0).
 template <typename T, int DM>
-void* spmv_kernel(const fsim_sim* s, bool zd) {
+void* spmv_kernel(const fsim_sim* s, bool zd, int n_pleaf) {
   if constexpr (std::is_same<T, float>::value) {
+    if (use_tma_spmv<T>(s, n_pleaf)) {
+      void* fn = zd ? reinterpret_cast<void*>(k_pcg_spmv_tma<DM, true>)
+                    : reinterpret_cast<void*>(k_pcg_spmv_tma<DM, false>);
+      // opt in to the ring's dynamic shared memory (idempotent)
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaDynSmem));
+      return fn;
+    }
     if (s->use_pipe)
       return zd ? reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM, true>)
                 : reinterpret_cast<void*>(k_pcg_spmv_pl<T, DM, false>);
   }
   return reinterpret_cast<void*>(k_pcg_spmv<T, DM>);
+}
+// dynamic shared memory of the spmv launch
+template <typename T>
+size_t spmv_smem(const fsim_sim* s, int n_pleaf) {
+  return use_tma_spmv<T>(s, n_pleaf) ? kTmaDynSmem : 0;
 }
 template <typename T, int DM>
 void* update_kernel(const fsim_sim* s, bool zd) {
@@ -1482,10 +1729,11 @@ bool use_zdirect(const fsim_sim* s, int n_pleaf) {
   return std::is_same<T, float>::value && s->use_pipe &&
          (s->zdirect > 0 || (s->zdirect < 0 && n_pleaf > kZDirectLeaves));
 }
-int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a) {
+int launch_hot(fsim_sim* s, const char* name, void* fn, int grid, PcgArgs& a,
+               size_t smem = 0) {
   fsim::ProfScope ps(s, name);
   void* args[] = {&a};
-  const cudaError_t e = cudaLaunchKernel(fn, dim3(unsigned(grid)), dim3(kHotThreads), args, 0,
+  const cudaError_t e = cudaLaunchKernel(fn, dim3(unsigned(grid)), dim3(kHotThreads), args, smem,
                                          s->stream);
   s->launches++;
   if (e != cudaSuccess) return cuda_fail(s, e, name);
@@ -1549,7 +1797,9 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pa
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
       const bool zd = use_zdirect<T>(s, a.n_pleaf);
-      kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s, zd) : spmv_kernel<T, DM>(s, zd);
+      kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s, zd)
+                               : spmv_kernel<T, DM>(s, zd, a.n_pleaf);
+      kn.kernel.sharedMemBytes = (k & 1) ? 0u : unsigned(spmv_smem<T>(s, a.n_pleaf));
       cudaGraphEdgeData ed = {};
       if (pdl) {  // the successor may launch while this kernel's last CTAs finish
         ed.from_port = cudaGraphKernelNodePortProgrammatic;
@@ -1612,9 +1862,10 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   const int wpb = kHotThreads / 32;
   int occ_a = 1, occ_b = 1;
   const bool zd = use_zdirect<T>(s, a.n_pleaf);
-  void* const fn_spmv = spmv_kernel<T, DM>(s, zd);
+  void* const fn_spmv = spmv_kernel<T, DM>(s, zd, a.n_pleaf);
   void* const fn_upd = update_kernel<T, DM>(s, zd);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, fn_spmv, kHotThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, fn_spmv, kHotThreads,
+                                                spmv_smem<T>(s, a.n_pleaf));
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, fn_upd, kHotThreads, 0);
   const int resident = std::max(1, std::min(occ_a, occ_b)) * s->num_sms;
   const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb, resident,
@@ -1627,7 +1878,9 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     // which prefetch before their wait; the others wait at their first
     // instruction, and their early-launched CTAs only hold SM slots (the
     // FP64 solve measured 20% slower with them).
-    const bool pdl = s->use_pdl && std::is_same<T, float>::value && s->use_pipe;
+    // (the bulk-copy spmv also waits at its first instruction)
+    const bool pdl = s->use_pdl && std::is_same<T, float>::value && s->use_pipe &&
+                     !use_tma_spmv<T>(s, a.n_pleaf);
     const int pass_iters = pass_iters_for(s);
     if (pdl) {
       rc = run_graph_loop<T, DM>(s, a, wgrid, par0, true, pass_iters);
@@ -1645,6 +1898,8 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
       const int64_t n = std::max(s->h_sc->iter - it0, 0);
       s->launches += 2 * pass_iters * (n / pass_iters + 1);
       s->pcg_seg_max = std::max(s->pcg_seg_max, int(std::min<int64_t>(n, 1 << 30)));
+      if (s->h_sc->wait_err)
+        return fail(s, FSIM_ERR_TIMEOUT, "PCG: a bulk-copy stage wait gave up");
       return FSIM_OK;
     }
     s->use_graphs = false;  // fall back for the rest of this handle's life
@@ -1660,13 +1915,14 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
     if (s->h_sc->done) break;
     for (int c = 0; c < chunk; ++c, ++launched) {
       a.par = int(launched & 1);
-      int rc = launch_hot(s, nm_spmv, fn_spmv, wgrid, a);
+      int rc = launch_hot(s, nm_spmv, fn_spmv, wgrid, a, spmv_smem<T>(s, a.n_pleaf));
       if (rc == FSIM_OK) rc = launch_hot(s, nm_upd, fn_upd, wgrid, a);
       if (rc != FSIM_OK) return rc;
     }
     if (chunk < 64) chunk *= 2;
   }
   lt.stop();
+  if (s->h_sc->wait_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG: a bulk-copy stage wait gave up");
   return FSIM_OK;
 }
 
@@ -1718,6 +1974,8 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
   a.x64 = s->x64;
   a.dinner = s->pres;
   a.init_r = 1;
+  a.withhold = s->tma_withhold;
+  s->tma_withhold = 0;  // a test's withheld copy applies to one solve
 
   PcgScalars h;
   memset(&h, 0, sizeof(h));

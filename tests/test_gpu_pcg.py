@@ -140,11 +140,14 @@ def test_mixed_segments_stop_at_the_outer_target():
 
 def test_loop_variants_agree(monkeypatch):
     """The graph loop (plain or programmatic edges), host polling, the
-    unpipelined kernels and the direct z-face reads run the same arithmetic
-    in the same order: bitwise equal solves."""
+    unpipelined kernels, the direct z-face reads and the bulk-copy staged
+    spmv (with z-face planes or direct reads) run the same arithmetic in the
+    same order: bitwise equal solves."""
     variants = (("graph", {}), ("host", {"FSIM_PCG_GRAPH": "0"}),
                 ("unpiped", {"FSIM_PCG_PIPE": "0"}), ("plain_edges", {"FSIM_PCG_PDL": "0"}),
-                ("zdirect", {"FSIM_PCG_ZDIRECT": "1"}))
+                ("zdirect", {"FSIM_PCG_ZDIRECT": "1"}), ("tma", {"FSIM_PCG_TMA": "1"}),
+                ("tma_host", {"FSIM_PCG_TMA": "1", "FSIM_PCG_GRAPH": "0"}),
+                ("tma_zdirect", {"FSIM_PCG_TMA": "1", "FSIM_PCG_ZDIRECT": "1"}))
     solves = ((fsim.PREC_FP32, 1e-5), (fsim.PREC_MIXED, 1e-7), (fsim.PREC_FP64, 1e-7))
     got = {}
     for name, env in variants:
@@ -163,6 +166,34 @@ def test_loop_variants_agree(monkeypatch):
         for name, _ in variants[1:]:
             it2, rr2, x2 = got[name, prec]
             assert it2 == it and rr2 == rr and np.array_equal(x2, x), (name, prec)
+
+
+def test_bulk_copy_wait_gives_up_and_recovers(monkeypatch):
+    """The bulk-copy spmv's stage waits are bounded.  With
+    FSIM_PCG_TMA_WITHHOLD=1 the first solve's spmv launches hold back one
+    stage's flags copy, so that stage's wait gives up (no fault: nothing is
+    in flight that the wait could miss); the kernel records FSIM_ERR_TIMEOUT,
+    completes the stage and carries on.  The solve reports FSIM_ERR_TIMEOUT,
+    and the handle's next solve runs normally, bit for bit as a handle that
+    never timed out."""
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 3000, tolerance=1e-5)
+    orc, ref = _prepared()
+    st_ref = ref.pcg_solve(prm)
+    x_ref = ref.field(fsim.FIELD_PRESSURE)[0]
+    ref.close()
+    for mode in ("1", "0"):  # graph loop, then host-polled launches
+        with monkeypatch.context() as m:
+            m.setenv("FSIM_PCG_TMA", "1")
+            m.setenv("FSIM_PCG_TMA_WITHHOLD", "1")
+            m.setenv("FSIM_PCG_GRAPH", mode)
+            orc, sim = _prepared()
+        with pytest.raises(fsim.FsimError) as err:
+            sim.pcg_solve(prm)
+        assert err.value.code == fsim.ERR_TIMEOUT
+        st = sim.pcg_solve(prm)  # the withheld copy applied to one solve only
+        assert st.status == 0 and st.iterations == st_ref.iterations
+        assert np.array_equal(sim.field(fsim.FIELD_PRESSURE)[0], x_ref)
+        sim.close()
 
 
 @pytest.mark.parametrize("n", [24, 64])
