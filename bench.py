@@ -62,16 +62,20 @@ ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update
 #   p = z + b p:                      read z, p; write p                      = 12 B
 # (fp32 vectors), keyed by the spmv kernel of the pair.
 UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50}
-# DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum, caches
-# flushed before the launch) from ncu captures of `bench.py --pcg-micro`: the fp32 pair on
-# the 256^3 dam-break system (4.02 M unknowns); scaled by each step's unknowns.
-NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": 49.94e6 / 4021250, "pcg_update": 61.35e6 / 4021250,
-                           # the MIXED pair from a capture at 1024^3 (111,452,816 unknowns),
-                           # the size its solver is benchmarked at
+# DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of `bench.py --pcg-micro`.  The fp32 pair: the 256^3 dam-break system (4,021,250
+# unknowns), host-launched loop (FSIM_PCG_GRAPH=0), caches NOT flushed between launches
+# (--cache-control none), 20 launches in the middle of the step's solve: the steady state of
+# the timed loop, where the vectors stay in L2 and DRAM mostly sees write-backs.  Scaled by
+# each step's unknowns.  The MIXED pair: a capture at 1024^3 (111,452,816 unknowns, caches
+# flushed; the vectors do not fit in L2 there), the size its solver is benchmarked at.
+NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": (1.4706e6 + 17.5451e6) / 4021250,
+                           "pcg_update": (5.4866e6 + 19.9465e6) / 4021250,
                            "pcg_spmv_mixed": 1.5765e9 / 111452816,
                            "pcg_update_mixed": 2.3834e9 / 111452816}
-NCU_TRAFFIC_SOURCE = {"pcg_spmv": "256^3", "pcg_update": "256^3",
-                      "pcg_spmv_mixed": "1024^3", "pcg_update_mixed": "1024^3"}
+NCU_TRAFFIC_SOURCE = {"pcg_spmv": "256^3, caches not flushed", "pcg_update": "256^3, caches not flushed",
+                      "pcg_spmv_mixed": "1024^3, caches flushed",
+                      "pcg_update_mixed": "1024^3, caches flushed"}
 # The two launches of one PCG iteration (spmv then update) are reported as one unit: the
 # split of the iteration's work between them is a design choice (the update could take
 # x += alpha p or leave it), and their times are nearly equal.
