@@ -37,6 +37,7 @@ import pytest
 
 import fsim
 from _util import FIELD_RTOL, assert_marker, make_gpu, make_oracle, rel_l2
+from oracle import oracle as O
 from oracle.oracle import OracleSim, compute_dt
 
 pytestmark = pytest.mark.gpu
@@ -56,7 +57,16 @@ def _replay(n, scene, steps, max_iterations, gpu_ref=False):
     step against the converged step.  The converged step comes from the
     oracle with the FP64 solver, or with gpu_ref from the GPU with its FP64
     solver (checked against the oracle's fp64 solve in tests/test_gpu_pcg.py),
-    which keeps the 256^3 case within a minute."""
+    which keeps the large cases within minutes.  The oracle runs on every
+    host thread (its results do not depend on the thread count)."""
+    O.set_threads(os.cpu_count() or 1)
+    try:
+        return _replay_steps(n, scene, steps, max_iterations, gpu_ref)
+    finally:
+        O.set_threads(1)
+
+
+def _replay_steps(n, scene, steps, max_iterations, gpu_ref):
     orc = make_oracle(n, scene)
     sim = make_gpu(orc)
     g, f = fsim.physical_gravity(n)
@@ -133,7 +143,15 @@ def test_c0_sphere_drop_64_twenty_steps():
     _check(_replay(64, "sphere_drop", 20, 200), "C0 sphere_drop_64")
 
 
-def test_c1_dam_break_256_one_step():
-    """C1: the 256^3 dam break (x < 0.4, y < 0.6), 32.2 M particles, first
-    step, PCG relative 1e-5 (max 1500)."""
-    _check(_replay(256, "dam_break", 1, 1500, gpu_ref=True), "C1 dam_break_256")
+def test_c1_dam_break_256_three_steps():
+    """C1: the 256^3 dam break (x < 0.4, y < 0.6), 32.2 M particles, the
+    first three steps, PCG relative 1e-5 (max 1500)."""
+    _check(_replay(256, "dam_break", 3, 1500, gpu_ref=True), "C1 dam_break_256")
+
+
+def test_c2_multidam_512_one_step():
+    """C2's scene: the 512^3 multi-dam (four 0.2 x 0.5 x 0.2 blocks at the
+    x/z quadrant corners over a pool y < 0.05), 131 M particles, about 14% of
+    the leaves active, first step, with the benchmark's fp32 solver (PCG
+    relative 1e-5, max 1500)."""
+    _check(_replay(512, "multidam", 1, 1500, gpu_ref=True), "C2 multidam_512")
