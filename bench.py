@@ -305,7 +305,13 @@ def run_gpu(args, rank, world):
     e2e_split = {name: sum(m[i].elapsed_time(m[i + 1]) for m in marks) / e2e_steps
                  for i, name in enumerate(("upload_ms", "step_ms", "download_ms"))}
     # (b) the headline: fsim_step_host, one call per step with the copies
-    # overlapping the step (in place on the same pinned buffers)
+    # overlapping the step (in place on the same pinned buffers).  One untimed
+    # call first: its first use sets up the I/O stream and the staging buffer
+    # of the early position download (one-time allocations).
+    st, cnt = sim.step_host(next_dt(), prm, hp, hv, hg, out=(hp, hv, hg))
+    inv = st.next_inv_speed
+    if cnt < hp.shape[0]:
+        hp, hv, hg = hp[:cnt], hv[:cnt], hg[:cnt]
     barrier()
     torch.cuda.synchronize()
     e0.record(stream)
@@ -716,7 +722,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-5)
     ap.add_argument("--max-iterations", type=int, default=1500)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-pcg-iters", type=int, default=40)
     ap.add_argument("--profile-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
