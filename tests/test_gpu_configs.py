@@ -1,4 +1,4 @@
-"""GPU parity on the benchmark configurations, with the production solver.
+"""GPU parity on the benchmark scenes, with the production solver.
 
 The other parity tests solve the pressure to convergence on both sides.  Here
 both sides run the solver the benchmark runs: fp32 Jacobi PCG to relative
@@ -136,22 +136,22 @@ def _check(rows, label):
             assert e["d"] <= FIELD_RTOL + e["e_gpu"] + e["e_orc"], (name, r)
 
 
-def test_c0_sphere_drop_64_twenty_steps():
-    """C0: 64^3 sphere drop (r 0.15 at (0.5, 0.7, 0.5) over a pool y < 0.2),
+def test_sphere_drop_64_twenty_steps():
+    """The 64^3 sphere drop (r 0.15 at (0.5, 0.7, 0.5) over a pool y < 0.2),
     8 particles per cell from seed 0, walls, 20 steps, PCG relative 1e-5 with
     at most 200 iterations."""
-    _check(_replay(64, "sphere_drop", 20, 200), "C0 sphere_drop_64")
+    _check(_replay(64, "sphere_drop", 20, 200), "sphere_drop_64")
 
 
-def test_c1_dam_break_256_three_steps():
-    """C1: the 256^3 dam break (x < 0.4, y < 0.6), 32.2 M particles, the
+def test_dam_break_256_three_steps():
+    """The 256^3 dam break (x < 0.4, y < 0.6), 32.2 M particles, the
     first three steps, PCG relative 1e-5 (max 1500)."""
-    _check(_replay(256, "dam_break", 3, 1500, gpu_ref=True), "C1 dam_break_256")
+    _check(_replay(256, "dam_break", 3, 1500, gpu_ref=True), "dam_break_256")
 
 
-def test_c2_multidam_512_one_step():
-    """C2's scene: the 512^3 multi-dam (four 0.2 x 0.5 x 0.2 blocks at the
+def test_multidam_512_one_step():
+    """The 512^3 multi-dam of the mixed-precision comparison (four 0.2 x 0.5 x 0.2 blocks at the
     x/z quadrant corners over a pool y < 0.05), 131 M particles, about 14% of
     the leaves active, first step, with the benchmark's fp32 solver (PCG
     relative 1e-5, max 1500)."""
-    _check(_replay(512, "multidam", 1, 1500, gpu_ref=True), "C2 multidam_512")
+    _check(_replay(512, "multidam", 1, 1500, gpu_ref=True), "multidam_512")
