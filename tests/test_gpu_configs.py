@@ -150,8 +150,8 @@ def test_dam_break_256_three_steps():
 
 
 def test_multidam_512_one_step():
-    """The 512^3 multi-dam of the mixed-precision comparison (four 0.2 x 0.5 x 0.2 blocks at the
-    x/z quadrant corners over a pool y < 0.05), 131 M particles, about 14% of
-    the leaves active, first step, with the benchmark's fp32 solver (PCG
-    relative 1e-5, max 1500)."""
+    """The 512^3 multi-dam of the mixed-precision comparison (four
+    0.2 x 0.5 x 0.2 blocks at the x/z quadrant corners over a pool
+    y < 0.05), 131 M particles, about 14% of the leaves active, first step,
+    with the benchmark's fp32 solver (PCG relative 1e-5, max 1500)."""
     _check(_replay(512, "multidam", 1, 1500, gpu_ref=True), "multidam_512")
