@@ -55,13 +55,16 @@ WORKLOADS = {
 #   pcg_spmv:   read r, p_{j-1} (8) + flags (1); write p_j (4)        = 13 B
 #   pcg_update: read p_j, x, r (12) + flags (1); write x, r (8)       = 21 B
 ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update_mixed": 21,
-             "pcg_spmv_f64": 25, "pcg_update_f64": 41}
+             "pcg_spmv_f64": 25, "pcg_update_f64": 41,
+             # single-reduction iteration (FSIM_PCG_CG1=1): read flags, x, p, r, w, s;
+             # write x, p, r, w, s
+             "pcg_cg1": 41}
 # The same iteration in the textbook formulation, where z = M^-1 r and Ap are stored:
 #   Ap = A p and p.Ap:                read p, flags; write Ap                 =  9 B
 #   x += a p; r -= a Ap; z; r.r, r.z: read x, p, r, Ap, flags; write x, r, z  = 29 B
 #   p = z + b p:                      read z, p; write p                      = 12 B
 # (fp32 vectors), keyed by the spmv kernel of the pair.
-UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50}
+UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50, "pcg_cg1": 50}
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
 # captures of `bench.py --pcg-micro`.  The fp32 pair: the 256^3 dam-break system (4,021,250
 # unknowns), host-launched loop (FSIM_PCG_GRAPH=0), caches NOT flushed between launches
@@ -82,6 +85,8 @@ NCU_TRAFFIC_SOURCE = {"pcg_spmv": "256^3, caches not flushed", "pcg_update": "25
 PCG_PAIRS = {"pcg_spmv": "pcg_update", "pcg_update": "pcg_spmv",
              "pcg_spmv_mixed": "pcg_update_mixed", "pcg_update_mixed": "pcg_spmv_mixed",
              "pcg_spmv_f64": "pcg_update_f64", "pcg_update_f64": "pcg_spmv_f64"}
+# Kernels that are a whole PCG iteration on their own.
+PCG_SINGLE = {"pcg_cg1"}
 
 
 def peaks():
@@ -401,8 +406,10 @@ def roofline(res):
     top = max(kt.items(), key=lambda kv: kv[1][0])
     name, (tot_ms, nl) = top
     out = {"bound": "hbm", "peak": peak, "peak_source": src, "unit": "GB/s", "traffic": None}
-    if name in PCG_PAIRS and PCG_PAIRS[name] in kt and res.get("loop_ms") and sum(res["loop_ms"]) > 0:
-        names = sorted([name, PCG_PAIRS[name]], key=lambda k: "update" in k)  # spmv, update
+    pair = name in PCG_PAIRS and PCG_PAIRS[name] in kt
+    if (pair or name in PCG_SINGLE) and res.get("loop_ms") and sum(res["loop_ms"]) > 0:
+        # spmv, update; or the one kernel of a single-reduction iteration
+        names = sorted([name, PCG_PAIRS[name]], key=lambda k: "update" in k) if pair else [name]
         per = sum(ALG_BYTES[k] for k in names)
         its, rws, lms = res["iters"], res["rows"], res["loop_ms"]
         tot_bytes = sum(per * r * it for r, it in zip(rws, its))

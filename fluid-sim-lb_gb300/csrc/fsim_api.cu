@@ -195,7 +195,8 @@ int ensure_leaf_capacity(fsim_sim* s, int64_t n_gleaf, int64_t n_pleaf) {
     int64_t cap = std::min<int64_t>(int64_t(s->lm.dense) + 1,
                                     std::max<int64_t>((int64_t(n_pleaf) + 1) * 5 / 4, 64));
     dfree(s->d_cell_range); dfree(s->d_leaf_range);
-    dfree(s->div); dfree(s->pres); dfree(s->r); dfree(s->p[0]); dfree(s->p[1]); dfree(s->Ap);
+    dfree(s->div); dfree(s->pres); dfree(s->r); dfree(s->p[0]); dfree(s->p[1]);
+    for (int b = 0; b < 2; ++b) { dfree(s->cgw[b]); dfree(s->cgs[b]); }
     dfree(s->flags); dfree(s->x64); dfree(s->r64); dfree(s->p64[0]); dfree(s->p64[1]);
     dfree(s->Ap64); dfree(s->b64); dfree(s->zface); dfree(s->zface64); dfree(s->zflags);
     const size_t n = size_t(cap) * 512;
@@ -259,6 +260,14 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if (const char* c = std::getenv("FSIM_PCG_TMA_WITHHOLD")) s->tma_withhold = c[0] == '1';
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels
   if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
+  // FSIM_PCG_CG1=0/1: fp32 solves never / always by the single-reduction
+  // iteration (default: by system size)
+  if (const char* c = std::getenv("FSIM_PCG_CG1")) s->pcg_cg1 = c[0] == '1' ? 1 : 0;
+  {
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->dev);
+    s->l2_bytes = l2;
+  }
   for (int a = 0; a < 3; ++a) {
     s->lm.n[a] = cfg->global_dims[a];
     s->lm.lmax[a] = cfg->global_dims[a] / 8;
@@ -283,7 +292,7 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if ((rc = dmalloc(s, &s->d_cnt, 16))) return bail(rc);
   if ((rc = dmalloc(s, &s->d_sc, 1))) return bail(rc);
   if ((rc = dmalloc(s, &s->d_part, size_t(s->max_blocks) * 4))) return bail(rc);
-  if ((rc = dmalloc(s, &s->d_partf, size_t(s->max_blocks) * 8))) return bail(rc);
+  if ((rc = dmalloc(s, &s->d_partf, size_t(s->max_blocks) * 16))) return bail(rc);
   if (cudaMallocHost(&s->h_cnt, 16 * sizeof(int64_t)) != cudaSuccess) return bail(FSIM_ERR_CUDA);
   if (cudaMallocHost(&s->h_sc, sizeof(PcgScalars)) != cudaSuccess) return bail(FSIM_ERR_CUDA);
   cudaMemsetAsync(s->d_cnt, 0, 16 * sizeof(int64_t), s->stream);
@@ -307,7 +316,8 @@ int fsim_destroy(fsim_t* s) {
   dfree(s->d_cell_range); dfree(s->d_leaf_range);
   dfree(s->vel); dfree(s->vold); dfree(s->weight); dfree(s->vel_on); dfree(s->vold_on);
   dfree(s->marker); dfree(s->div); dfree(s->pres); dfree(s->r); dfree(s->p[0]); dfree(s->p[1]);
-  dfree(s->Ap); dfree(s->flags); dfree(s->zface); dfree(s->zface64); dfree(s->zflags);
+  for (int b = 0; b < 2; ++b) { dfree(s->cgw[b]); dfree(s->cgs[b]); }
+  dfree(s->flags); dfree(s->zface); dfree(s->zface64); dfree(s->zflags);
   dfree(s->x64); dfree(s->r64); dfree(s->p64[0]);
   dfree(s->p64[1]); dfree(s->Ap64); dfree(s->b64); dfree(s->d_sc); dfree(s->d_part);
   dfree(s->d_partf); dfree(s->d_cnt);

@@ -18,8 +18,8 @@
 //  * Grid fields are stored per slot as 512 voxels (offset x*64+y*8+z):
 //    velocity / saved velocity / weight as three 512-float planes per slot,
 //    active bits as 16 words per slot, the marker as one byte per voxel,
-//    and the PCG vectors (divergence, pressure, r, p, Ap, flags) per
-//    particle-leaf slot.
+//    and the PCG vectors (divergence, pressure, r, p, flags; w and s of
+//    the single-reduction iteration) per particle-leaf slot.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -142,9 +142,10 @@ __host__ __device__ inline int flag_diag(uint8_t f) { return (f >> 1) & 7; }
 
 // State handed from one hot PCG kernel to the next (see k_pcg.cu): the
 // residual dots and beta when they are given (after setup or a residual
-// replacement) instead of summed from the previous kernel's partials.
+// replacement) instead of summed from the previous kernel's partials.  The
+// single-reduction loop keeps gamma_{i-1} in rz_prev and alpha_{i-1} in alpha.
 struct PcgIterState {
-  double rr, rz, beta, rz_prev;
+  double rr, rz, beta, rz_prev, alpha;
   int iter, done, status, given;
 };
 
@@ -254,7 +255,9 @@ struct fsim_sim {
   float* pres = nullptr;  // x
   float* r = nullptr;
   float* p[2] = {nullptr, nullptr};
-  float* Ap = nullptr;
+  // single-reduction CG: w = A M r and s = A p, each double-buffered
+  float* cgw[2] = {nullptr, nullptr};
+  float* cgs[2] = {nullptr, nullptr};
   uint8_t* flags = nullptr;
   // z-face planes per particle leaf (z=0 and z=7, 64 cells each, x*8+y):
   // [r | p_a | p_b] planes and the flags planes, so that a leaf's -z / +z
@@ -270,7 +273,7 @@ struct fsim_sim {
   double* b64 = nullptr;
   fsim::PcgScalars* d_sc = nullptr;
   double* d_part = nullptr;  // block partials (3 * max_blocks)
-  float* d_partf = nullptr;  // fp32 / double-float partials of the hot PCG kernels (8 * max_blocks)
+  float* d_partf = nullptr;  // fp32 / double-float partials of the hot PCG kernels (16 * max_blocks)
   int max_blocks = 0;
 
   // misc device scalars: [0] n_live [1] n_pleaf [2] n_gleaf [3] invalid
@@ -305,6 +308,11 @@ struct fsim_sim {
   // register-pipelined hot kernels (next half leaf loaded during the
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;
+  // fp32 solves by the single-reduction (Chronopoulos-Gear) iteration, one
+  // kernel per iteration: -1 by system size (the systems whose vectors stay
+  // in L2), 0 never, 1 always (FSIM_PCG_CG1)
+  int pcg_cg1 = -1;
+  int64_t l2_bytes = 0;  // the device's L2 size
 
   // water sources and the time they see
   std::vector<fsim_source> sources;

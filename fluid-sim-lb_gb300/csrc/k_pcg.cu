@@ -11,7 +11,9 @@
 // the column order of the reference's sorted sparse rows (-x,-y,-z, diag,
 // +z,+y,+x), which makes it bit-identical to the oracle for identical p.
 //
-// Per iteration two kernels run back to back on device-resident scalars:
+// Per iteration two kernels run back to back on device-resident scalars
+// (fp32 solves of small systems run the single-reduction form below instead,
+// one kernel per iteration):
 //   spmv:   head: beta_{j-1} from the previous update's r.r, r.z partials
 //           and the loop test; then p_j = z_j + beta_{j-1} p_{j-1} (z =
 //           r/diag recomputed, never stored) and p_j.(A p_j) partials.
@@ -303,6 +305,8 @@ struct PcgArgs {
   int par;          // spmv / update: parity of the iteration this launch serves
   int withhold;     // bulk-copy spmv, test only: CTA 0's first stage withholds its flags copy
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
+  void* w[2];       // single-reduction CG: w = A M r (by parity), or null
+  void* sv[2];      // single-reduction CG: s = A p (by parity)
 };
 
 __device__ __forceinline__ bool converged(const PcgScalars* sc, double rr) {
@@ -335,6 +339,13 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
     for (int v = threadIdx.x; v < 384; v += kThreads)
       static_cast<T*>(a.zf)[int64_t(a.n_pleaf) * 384 + v] = T(0);
     for (int v = threadIdx.x; v < 128; v += kThreads) a.zff[int64_t(a.n_pleaf) * 128 + v] = 0;
+    if (a.w[0]) {  // the single-reduction loop's halo reads of w and s
+      for (int v = threadIdx.x; v < 512; v += kThreads)
+        for (int b = 0; b < 2; ++b) {
+          static_cast<T*>(a.w[b])[o + v] = T(0);
+          static_cast<T*>(a.sv[b])[o + v] = T(0);
+        }
+    }
   }
   Dot<DM> drr, drz, dbb;
   int nfluid = 0;
@@ -401,7 +412,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_setup(const __grid_constant__ 
     if (sc->mode == FSIM_PCG_RELATIVE) sc->thr = sc->tol2 * sc->bb;
     sc->done = (sc->max_iter <= 0) || converged(sc, sc->rr);
     // the first spmv takes r.r, r.z and beta = 0 from here
-    PcgIterState o;
+    PcgIterState o = {};
     o.rr = sc->rr;
     o.rz = sc->rz;
     o.beta = 0.0;
@@ -828,7 +839,7 @@ __device__ __forceinline__ HotHead update_head(HeadStage<1, PartT<DM>>& hs, cons
           sc->status = status;
           sc->done = 1;
         } else {
-          PcgIterState o;
+          PcgIterState o = {};
           o.rr = 0.0;
           o.rz = 0.0;
           o.beta = 0.0;
@@ -1581,6 +1592,243 @@ __global__ void __launch_bounds__(kHotThreads, 4)
   put_partials<DM, 2>(a, 0, v);
 }
 
+// ---- single-reduction CG (Chronopoulos-Gear) ----------------------------------
+// fp32 solves of systems whose vectors stay in L2 (use_cg1 below; forced on
+// or off by FSIM_PCG_CG1=1/0): one kernel per iteration instead of the
+// spmv / update pair, so one grid-wide dependency per iteration instead of
+// two.  With u = M r (recomputed, never stored), w = A u and
+// s = A p kept as vectors, the iteration takes both of its scalars from one
+// reduction, gamma_i = r_i.u_i and delta_i = w_i.u_i:
+//   beta_i  = gamma_i / gamma_{i-1}                 (0 at i = 0)
+//   alpha_i = gamma_i / (delta_i - beta_i gamma_i / alpha_{i-1})   (= r.z / p.Ap)
+//   p_i = u_i + beta_i p_{i-1};   s_i = w_i + beta_i s_{i-1}
+//   x += alpha_i p_i;   r_{i+1} = r_i - alpha_i s_i;   w_{i+1} = A M r_{i+1}
+// and the partials of gamma_{i+1}, delta_{i+1} and r_{i+1}.r_{i+1} (the loop
+// test of PCGDriver::Solve, common/solver_driver.cc:14-69, at the head of
+// the next launch).  In exact arithmetic these are the iterates of
+// common/solver.cc:297-366; the rounding differs (p.Ap is not formed
+// directly), so solves agree with the reference's to the solver tolerance,
+// not bitwise.
+//
+// w_{i+1} needs M r_{i+1} on the half leaf's halo: each lane recomputes
+// r_{i+1} there from r_i, w_i, s_{i-1} with the owner's operations (so the
+// owner's bits), which is why r, w and s alternate between two buffers by
+// launch parity, while x and p, read only at their own cells, are updated in
+// place.  The first launch of a solve (after setup) computes w_0 = A M r_0
+// with alpha = beta = 0 and w, s, p, x taken as 0.
+// Per unknown and iteration it reads flags, x, p, r, w, s and writes x, p, r,
+// w, s: 41 B, against the pair's 34 B.
+constexpr int kPartCg1 = 0;  // part[] rows: gamma, delta, r.r of launch parity 0, then of parity 1
+
+struct Cg1Head {
+  int done, init;
+  double alpha, beta;
+};
+
+// Head of a single-reduction launch: the predecessor's gamma, delta and r.r,
+// the loop test, then alpha and beta with the CHECK_LE(., LARGE_FLOAT) tests
+// of ComputeLocal2 / ComputeLocal3.  Launch parity par reads st[par ^ 1] and
+// CTA 0 writes st[par].
+template <int DM>
+__device__ __forceinline__ Cg1Head cg1_head(HeadStage<3, PartT<DM>>& hs, Cg1Head& out,
+                                            const PcgArgs& a) {
+  double acc[3];
+  head_sum<DM, 3>(hs, acc);
+  if (threadIdx.x == 0) {
+    const PcgScalars* cs = &hs.sc;
+    const int par = a.par;
+    const PcgIterState in = cs->st[par ^ 1];
+    Cg1Head o;
+    o.done = in.done;
+    o.init = 0;
+    o.alpha = 0.0;
+    o.beta = 0.0;
+    int status = in.status;
+    double rr = 0.0, gamma = 0.0, delta = 0.0;
+    if (!in.done && in.given) {
+      o.init = 1;  // after setup: this launch forms w_0
+    } else if (!in.done) {
+      gamma = round_t(cs, acc[0]);
+      delta = round_t(cs, acc[1]);
+      rr = round_t(cs, acc[2]);
+      const int i = in.iter;
+      if (i >= cs->max_iter || converged(cs, rr)) {
+        o.done = 1;
+      } else {
+        double alpha, beta = 0.0;
+        if (cs->fp32) {
+          const float g = float(gamma);
+          float den = float(delta);
+          if (i > 0) {
+            const float b = __fdiv_rn(g, float(in.rz_prev));
+            den = __fsub_rn(den, __fdiv_rn(__fmul_rn(b, g), float(in.alpha)));
+            beta = double(b);
+          }
+          alpha = double(__fdiv_rn(g, den));
+        } else {
+          double den = delta;
+          if (i > 0) {
+            beta = gamma / in.rz_prev;
+            den -= beta * gamma / in.alpha;
+          }
+          alpha = gamma / den;
+        }
+        if (!(beta <= 1e5) || !(alpha <= 1e5)) {
+          status = FSIM_ERR_BREAKDOWN;
+          o.done = 1;
+        }
+        o.alpha = alpha;
+        o.beta = beta;
+      }
+    }
+    if (blockIdx.x == 0) {
+      PcgScalars* sc = a.sc;
+      PcgIterState n = in;
+      if (!in.done) {
+        if (o.init) {
+          n.given = 0;
+          n.iter = 0;
+          n.rz_prev = 0.0;
+          n.alpha = 0.0;
+        } else {
+          sc->rr = rr;
+          sc->rz = gamma;
+          sc->pAp = delta;
+          sc->iter = in.iter;
+          sc->status = status;
+          if (o.done) {
+            n.done = 1;
+            n.status = status;
+            sc->done = 1;
+          } else {
+            n.rz_prev = gamma;
+            n.alpha = o.alpha;
+            n.iter = in.iter + 1;
+            sc->rz_old = in.rz_prev;
+            sc->alpha = o.alpha;
+            sc->beta = o.beta;
+          }
+        }
+      }
+      sc->st[par] = n;
+      if (o.done && a.cond) cudaGraphSetConditional(a.cond, 0u);
+    }
+    out = o;
+  }
+  __syncthreads();
+  return out;
+}
+
+// r_{i+1} of a cell from its r_i, w_i and s_{i-1}: the owner's operations
+// (s_i = w_i + beta s_{i-1}, then r_i - alpha s_i), for the halo.
+template <typename T>
+__device__ __forceinline__ T cg1_rnext(T r, T w, T s, T nalpha, T beta) {
+  return tadd(tmul(nalpha, tadd(w, tmul(beta, s))), r);
+}
+
+template <typename T, int DM>
+__global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  __shared__ HeadStage<3, PartT<DM>> hs;
+  __shared__ Cg1Head hout;
+  const int par = a.par;
+  const T* ra = static_cast<const T*>(par ? a.p1 : a.r);
+  T* rb = static_cast<T*>(par ? a.r : a.p1);
+  const T* wa = static_cast<const T*>(a.w[par]);
+  T* wb = static_cast<T*>(a.w[par ^ 1]);
+  const T* sa = static_cast<const T*>(a.sv[par]);
+  T* sb = static_cast<T*>(a.sv[par ^ 1]);
+  T* x = static_cast<T*>(a.x);
+  T* p = static_cast<T*>(a.p0);
+  const int lane = threadIdx.x & 31;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  fill_diag_table<T>(tab);
+  // before the wait: the neighbour table (fixed during the solve)
+  int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  pdl_wait();
+  pdl_trigger();
+  head_issue<DM, 3>(hs, a, kPartCg1 + 3 * (par ^ 1));
+  const Cg1Head head = cg1_head<DM>(hs, hout, a);
+  if (head.done) return;
+  const bool init = head.init != 0;
+  const T alpha = T(head.alpha), nalpha = -alpha, beta = T(head.beta);
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
+  Dot<DM> dg, dd, drr;
+  for (; hw < nhw; hw += hstride) {
+    const int nbl_next =
+        hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+    int fs[6];
+    face_slots(nbl, fs);
+    nbl = nbl_next;
+    const HalfLeaf h = half_pos(hw, lane);
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
+    // own column
+    const uint2 f = ldflags(a.flags, o);
+    Col<T> R, W, S, P, X;
+    ldcol(ra, o, R);
+    ldcol(wa, o, W);
+    ldcol(sa, o, S);
+    ldcol(p, o, P);
+    ldcol(x, o, X);
+    // halo column (the zeroed null slot when there is none)
+    int hslot, hvox;
+    halo_col(h, fs, hslot, hvox);
+    const unsigned hb = slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox);
+    const uint2 hf = ldflags(a.flags, hb);
+    Col<T> HR, HW, HS;
+    ldcol(ra, hb, HR);
+    ldcol(wa, hb, HW);
+    ldcol(sa, hb, HS);
+    // z faces: the -z leaf's z = 7 cell and the +z leaf's z = 0 cell, read
+    // from the vectors (published z-face planes of r, w and s measured slower)
+    const unsigned z0 = slot_or_null(fs[4], a.n_pleaf) * 512u + unsigned(h.c) + 7u;
+    const unsigned z1 = slot_or_null(fs[5], a.n_pleaf) * 512u + unsigned(h.c);
+    const uint8_t zg0 = ldv(a.flags + z0), zg1 = ldv(a.flags + z1);
+    const T zr0 = ldv(ra + z0), zr1 = ldv(ra + z1);
+    T zw0 = ldv(wa + z0), zw1 = ldv(wa + z1), zs0 = ldv(sa + z0), zs1 = ldv(sa + z1);
+    if (init) {
+#pragma unroll
+      for (int z = 0; z < 8; ++z) W.v[z] = S.v[z] = P.v[z] = X.v[z] = HW.v[z] = HS.v[z] = T(0);
+      zw0 = zw1 = zs0 = zs1 = T(0);
+    }
+    Col<T> U, HU;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      const T inv = tab[fbyte(f, z) & 15].inv;
+      P.v[z] = tadd(tmul(inv, R.v[z]), tmul(beta, P.v[z]));
+      S.v[z] = tadd(W.v[z], tmul(beta, S.v[z]));
+      X.v[z] = tadd(tmul(alpha, P.v[z]), X.v[z]);
+      R.v[z] = tadd(tmul(nalpha, S.v[z]), R.v[z]);
+      U.v[z] = tmul(inv, R.v[z]);
+      HU.v[z] = tmul(tab[fbyte(hf, z) & 15].inv, cg1_rnext(HR.v[z], HW.v[z], HS.v[z], nalpha, beta));
+    }
+    const T zm = tmul(tab[zg0 & 15].inv, cg1_rnext(zr0, zw0, zs0, nalpha, beta));
+    const T zp = tmul(tab[zg1 & 15].inv, cg1_rnext(zr1, zw1, zs1, nalpha, beta));
+    __syncwarp();  // previous half leaf's tile reads are done
+    st_col_sh(tile, h.lx + 1, h.cy + 1, U);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, HU);
+    __syncwarp();
+    Col<T> WN;
+    stencil_col<T>(tile, tab, h.lx, h.cy, U, f, zm, zp, WN);
+#pragma unroll
+    for (int z = 0; z < 8; ++z) {
+      dg.add(R.v[z], U.v[z]);
+      dd.add(WN.v[z], U.v[z]);
+      drr.add(R.v[z], R.v[z]);
+    }
+    stcol(p, o, P);
+    stcol(x, o, X);
+    stcol(sb, o, S);
+    stcol(rb, o, R);
+    stcol(wb, o, WN);
+  }
+  PartT<DM> v[3] = {dg.pvalue(), dd.pvalue(), drr.pvalue()};
+  put_partials<DM, 3>(a, kPartCg1 + 3 * par, v);
+}
+
 // MIXED: x64 += d (inner solution); d is the fp32 x of the inner solve.
 __global__ void k_accumulate_x64(const __grid_constant__ PcgArgs a) {
   const int64_t n = int64_t(a.n_pleaf) * 512;
@@ -1661,7 +1909,7 @@ __global__ void __launch_bounds__(kThreads) k_pcg_replace(const __grid_constant_
     sc->status = FSIM_OK;
     sc->done = (sc->iter >= sc->max_iter) ? 1 : 0;
     // the resuming spmv takes r'.r', r'.z' and beta from here
-    PcgIterState o;
+    PcgIterState o = {};
     o.rr = sc->rr;
     o.rz = sc->rz;
     o.beta = sc->beta;
@@ -1768,8 +2016,12 @@ int pass_iters_for(const fsim_sim* s) {
   return p >= 32.0 ? 32 : (p >= 16.0 ? 16 : 8);
 }
 
+//
+// With fn_cg1 (the single-reduction kernel) the body is pass_iters launches
+// of that kernel, one per iteration, alternating parity.
 template <typename T, int DM>
-int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pass_iters) {
+int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pass_iters,
+                   void* fn_cg1 = nullptr) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -1789,17 +2041,23 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pa
     ap[0].par = par0;
     ap[1].par = par0 ^ 1;
     cudaGraphNode_t prev = nullptr;
-    for (int k = 0; k < 2 * pass_iters && e == cudaSuccess; ++k) {
+    const int nodes = fn_cg1 ? pass_iters : 2 * pass_iters;
+    for (int k = 0; k < nodes && e == cudaSuccess; ++k) {
       cudaGraphNodeParams kn = {};
       kn.type = cudaGraphNodeTypeKernel;
-      void* args[] = {&ap[(k >> 1) & 1]};
+      void* args[] = {&ap[fn_cg1 ? (k & 1) : ((k >> 1) & 1)]};
       kn.kernel.gridDim = dim3(unsigned(wgrid));
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
       const bool zd = use_zdirect<T>(s, a.n_pleaf);
-      kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s, zd)
-                               : spmv_kernel<T, DM>(s, zd, a.n_pleaf);
-      kn.kernel.sharedMemBytes = (k & 1) ? 0u : unsigned(spmv_smem<T>(s, a.n_pleaf));
+      if (fn_cg1) {
+        kn.kernel.func = fn_cg1;
+        kn.kernel.sharedMemBytes = 0u;
+      } else {
+        kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s, zd)
+                                 : spmv_kernel<T, DM>(s, zd, a.n_pleaf);
+        kn.kernel.sharedMemBytes = (k & 1) ? 0u : unsigned(spmv_smem<T>(s, a.n_pleaf));
+      }
       cudaGraphEdgeData ed = {};
       if (pdl) {  // the successor may launch while this kernel's last CTAs finish
         ed.from_port = cudaGraphKernelNodePortProgrammatic;
@@ -1926,8 +2184,85 @@ int run_inner(fsim_sim* s, PcgArgs& a, int grid, const char* nm_setup, const cha
   return FSIM_OK;
 }
 
+// One fp32 solve by the single-reduction iteration: setup, the launch that
+// forms w_0 = A M r_0, then the iterations, as run_inner runs them (a graph
+// WHILE loop, or host-polled chunks).
+template <typename T, int DM>
+int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
+  a.cond = 0;
+  FSIM_LAUNCH(s, "pcg_setup", (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
+  void* const fn = reinterpret_cast<void*>(k_pcg_cg1<T, DM>);
+  const int wpb = kHotThreads / 32;
+  int occ = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kHotThreads, 0);
+  const int wgrid = std::max(1, std::min({(2 * a.n_pleaf + wpb - 1) / wpb,
+                                          std::max(1, occ) * s->num_sms, s->max_blocks,
+                                          kMaxHotGrid}));
+  a.par = 0;
+  int rc = launch_hot(s, "pcg_cg1", fn, wgrid, a);
+  if (rc != FSIM_OK) return rc;
+  if (s->use_graphs && !s->profiling) {
+    LoopTimer lt(s);
+    const int pass_iters = pass_iters_for(s);
+    rc = FSIM_ERR_CUDA;
+    if (s->use_pdl) {
+      rc = run_graph_loop<T, DM>(s, a, wgrid, 1, true, pass_iters, fn);
+      if (rc != FSIM_OK) s->use_pdl = false;
+    }
+    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, 1, false, pass_iters, fn);
+    if (rc == FSIM_OK) {
+      lt.stop();
+      FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                 s->stream));
+      FSIM_CK(s, cudaStreamSynchronize(s->stream));
+      // one launch per iteration; the stop is set in the head of launch n
+      const int64_t n = std::max(s->h_sc->iter, 0);
+      s->launches += pass_iters * (n / pass_iters + 1);
+      s->pcg_seg_max = std::max(s->pcg_seg_max, int(std::min<int64_t>(n, 1 << 30)));
+      return FSIM_OK;
+    }
+    s->use_graphs = false;
+  }
+  a.cond = 0;
+  int chunk = 8;
+  int64_t launched = 1;
+  LoopTimer lt(s);
+  for (;;) {
+    FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                               s->stream));
+    FSIM_CK(s, cudaStreamSynchronize(s->stream));
+    if (s->h_sc->done) break;
+    for (int c = 0; c < chunk; ++c, ++launched) {
+      a.par = int(launched & 1);
+      if ((rc = launch_hot(s, "pcg_cg1", fn, wgrid, a)) != FSIM_OK) return rc;
+    }
+    if (chunk < 64) chunk *= 2;
+  }
+  lt.stop();
+  return FSIM_OK;
+}
+
+// fp32 solves take the single-reduction iteration when its working set (x,
+// p, r, w, s with r, w, s double-buffered, and the flags: 33 B per cell)
+// fits in half of the L2.  It saves one launch's fixed cost per iteration
+// (5.1 against 7.0 us per iteration at 64^3, 9.9 against 12.5 at 128^3), but
+// moves 41 B per unknown against the pair's 34: on systems whose vectors
+// spill from L2 it streams them from DRAM and is slower (35.3 against 32.1
+// us at 256^3, 122.5 against 120.6 at 512^3).
+bool use_cg1(const fsim_sim* s, int precision) {
+  if (precision != FSIM_PREC_FP32) return false;
+  if (s->pcg_cg1 >= 0) return s->pcg_cg1 > 0;
+  return double(s->n_pleaf) * 512.0 * 33.0 <= 0.5 * double(s->l2_bytes);
+}
+
 int ensure_pcg_vectors(fsim_sim* s, int precision) {
   const size_t n = size_t(s->cap_pleaf) * 512;
+  if (use_cg1(s, precision) && !s->cgw[0]) {
+    for (int b = 0; b < 2; ++b) {
+      FSIM_CK(s, cudaMalloc(&s->cgw[b], n * sizeof(float)));
+      FSIM_CK(s, cudaMalloc(&s->cgs[b], n * sizeof(float)));
+    }
+  }
   if (precision == FSIM_PREC_MIXED && !s->x64) FSIM_CK(s, cudaMalloc(&s->x64, n * sizeof(double)));
   if (precision == FSIM_PREC_FP64 && !s->r64) {
     if (!s->x64) FSIM_CK(s, cudaMalloc(&s->x64, n * sizeof(double)));
@@ -2001,7 +2336,13 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
     *s->h_sc = h;
     FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
                                s->stream));
-    if (prm->precision == FSIM_PREC_FP32)
+    if (use_cg1(s, prm->precision)) {
+      for (int b = 0; b < 2; ++b) {
+        a.w[b] = s->cgw[b];
+        a.sv[b] = s->cgs[b];
+      }
+      rc = run_cg1<float, 0>(s, a, grid);
+    } else if (prm->precision == FSIM_PREC_FP32)
       rc = run_inner<float, 0>(s, a, grid, "pcg_setup", "pcg_spmv", "pcg_update");
     else
       rc = run_inner<double, 2>(s, a, grid, "pcg_setup_f64", "pcg_spmv_f64", "pcg_update_f64");

@@ -12,6 +12,14 @@ from _util import make_gpu, make_oracle, rel_l2
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _pair_loop(monkeypatch):
+    """These tests cover the spmv / update pair: fp32 solves of systems this
+    small would otherwise take the single-reduction loop
+    (tests/test_gpu_pcg_cg1.py)."""
+    monkeypatch.setenv("FSIM_PCG_CG1", "0")
+
+
 def _prepared(n=32, scene="dam_break", noise=True):
     orc = make_oracle(n, scene, noise=0.3 * n if noise else 0.0)
     sim = make_gpu(orc)
