@@ -260,14 +260,8 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if (const char* c = std::getenv("FSIM_PCG_TMA_WITHHOLD")) s->tma_withhold = c[0] == '1';
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels
   if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
-  // FSIM_PCG_CG1=0/1: fp32 solves never / always by the single-reduction
-  // iteration (default: by system size)
+  // FSIM_PCG_CG1=1: fp32 solves by the single-reduction iteration (opt-in)
   if (const char* c = std::getenv("FSIM_PCG_CG1")) s->pcg_cg1 = c[0] == '1' ? 1 : 0;
-  {
-    int l2 = 0;
-    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, s->dev);
-    s->l2_bytes = l2;
-  }
   for (int a = 0; a < 3; ++a) {
     s->lm.n[a] = cfg->global_dims[a];
     s->lm.lmax[a] = cfg->global_dims[a] / 8;

@@ -309,10 +309,8 @@ struct fsim_sim {
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;
   // fp32 solves by the single-reduction (Chronopoulos-Gear) iteration, one
-  // kernel per iteration: -1 by system size (the systems whose vectors stay
-  // in L2), 0 never, 1 always (FSIM_PCG_CG1)
-  int pcg_cg1 = -1;
-  int64_t l2_bytes = 0;  // the device's L2 size
+  // kernel per iteration (FSIM_PCG_CG1=1; opt-in)
+  int pcg_cg1 = 0;
 
   // water sources and the time they see
   std::vector<fsim_source> sources;

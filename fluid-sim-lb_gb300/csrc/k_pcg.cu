@@ -12,8 +12,8 @@
 // +z,+y,+x), which makes it bit-identical to the oracle for identical p.
 //
 // Per iteration two kernels run back to back on device-resident scalars
-// (fp32 solves of small systems run the single-reduction form below instead,
-// one kernel per iteration):
+// (FSIM_PCG_CG1=1 runs fp32 solves by the single-reduction form below
+// instead, one kernel per iteration):
 //   spmv:   head: beta_{j-1} from the previous update's r.r, r.z partials
 //           and the loop test; then p_j = z_j + beta_{j-1} p_{j-1} (z =
 //           r/diag recomputed, never stored) and p_j.(A p_j) partials.
@@ -1593,10 +1593,9 @@ __global__ void __launch_bounds__(kHotThreads, 4)
 }
 
 // ---- single-reduction CG (Chronopoulos-Gear) ----------------------------------
-// fp32 solves of systems whose vectors stay in L2 (use_cg1 below; forced on
-// or off by FSIM_PCG_CG1=1/0): one kernel per iteration instead of the
-// spmv / update pair, so one grid-wide dependency per iteration instead of
-// two.  With u = M r (recomputed, never stored), w = A u and
+// Opt-in for fp32 solves (FSIM_PCG_CG1=1; use_cg1 below): one kernel per
+// iteration instead of the spmv / update pair, so one grid-wide dependency
+// per iteration instead of two.  With u = M r (recomputed, never stored), w = A u and
 // s = A p kept as vectors, the iteration takes both of its scalars from one
 // reduction, gamma_i = r_i.u_i and delta_i = w_i.u_i:
 //   beta_i  = gamma_i / gamma_{i-1}                 (0 at i = 0)
@@ -2242,17 +2241,16 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
   return FSIM_OK;
 }
 
-// fp32 solves take the single-reduction iteration when its working set (x,
-// p, r, w, s with r, w, s double-buffered, and the flags: 33 B per cell)
-// fits in half of the L2.  It saves one launch's fixed cost per iteration
-// (5.1 against 7.0 us per iteration at 64^3, 9.9 against 12.5 at 128^3), but
-// moves 41 B per unknown against the pair's 34: on systems whose vectors
-// spill from L2 it streams them from DRAM and is slower (35.3 against 32.1
-// us at 256^3, 122.5 against 120.6 at 512^3).
+// fp32 solves take the single-reduction iteration on request (FSIM_PCG_CG1=1).
+// It saves one launch's fixed cost per iteration (5.1 against 7.0 us per
+// iteration at 64^3, 9.9 against 12.5 at 128^3) but moves 41 B per unknown
+// against the pair's 34, which spill from L2 on larger systems (35.3 against
+// 32.1 us at 256^3).  Its recursively updated s = A p drifts from A p, so at
+// the reference's stopping rule its solution ends further from the converged
+// one than the pair's (pressure 7.8e-6 against 3.1e-6 after the first 64^3
+// sphere-drop step): the pair stays the default.
 bool use_cg1(const fsim_sim* s, int precision) {
-  if (precision != FSIM_PREC_FP32) return false;
-  if (s->pcg_cg1 >= 0) return s->pcg_cg1 > 0;
-  return double(s->n_pleaf) * 512.0 * 33.0 <= 0.5 * double(s->l2_bytes);
+  return precision == FSIM_PREC_FP32 && s->pcg_cg1 == 1;
 }
 
 int ensure_pcg_vectors(fsim_sim* s, int precision) {

@@ -1,7 +1,7 @@
 """The single-reduction (Chronopoulos-Gear) PCG loop.
 
-fp32 solves take it when its vectors fit in half of the L2 (FSIM_PCG_CG1=1
-forces it, =0 forbids it).  It runs the iterates of PCGSolver
+fp32 solves take it with FSIM_PCG_CG1=1 (the pair of kernels is the
+default).  It runs the iterates of PCGSolver
 (common/solver.cc:297-366) with one reduction per iteration: alpha from
 gamma = r.z and delta = (A z).z, and A p carried by a recurrence instead of
 formed from p.  In exact arithmetic the iterates are the reference's; in
@@ -128,29 +128,14 @@ def _loop_kernels(sim, prm):
     return names
 
 
-def test_chosen_by_system_size(monkeypatch):
-    """Without FSIM_PCG_CG1 the single-reduction loop runs the fp32 solves
-    of systems whose 33 B per cell fit in half of the L2 (a 32^3 dam break),
-    and the pair runs the larger ones (the 256^3 dam break, 4 M unknowns)
-    and every MIXED or FP64 solve."""
-    import torch
-
+def test_off_by_default(monkeypatch):
+    """Without FSIM_PCG_CG1 every solve runs the spmv / update pair."""
     monkeypatch.delenv("FSIM_PCG_CG1", raising=False)
-    l2 = torch.cuda.get_device_properties(0).L2_cache_size
-    prm = fsim.pcg_params(fsim.PCG_FIXED, fsim.PREC_FP32, 4)
     orc, sim = _prepared()
-    assert sim.leaves().shape[0] * 512 * 33 <= l2 / 2
-    assert "pcg_cg1" in _loop_kernels(sim, prm)
-    mixed = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_MIXED, 500, tolerance=1e-6)
-    assert "pcg_cg1" not in _loop_kernels(sim, mixed)
+    for prec in (fsim.PREC_FP32, fsim.PREC_MIXED):
+        names = _loop_kernels(sim, fsim.pcg_params(fsim.PCG_RELATIVE, prec, 500, tolerance=1e-5))
+        assert "pcg_cg1" not in names and any(k.startswith("pcg_spmv") for k in names), names
     sim.close()
-    n = 256
-    g, f = fsim.physical_gravity(n)
-    with fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f) as big:
-        big.seed(fsim.scene_passes("dam_break", n), seed=0)
-        big.transfer_particles_to_grid()
-        big.apply_boundary_conditions()
-        big.compute_divergence()
-        assert big.leaves().shape[0] * 512 * 33 > l2 / 2
-        names = _loop_kernels(big, prm)
-        assert "pcg_cg1" not in names and "pcg_spmv" in names
+    orc, sim = _prepared_cg1(monkeypatch)
+    assert "pcg_cg1" in _loop_kernels(sim, fsim.pcg_params(fsim.PCG_FIXED, fsim.PREC_FP32, 4))
+    sim.close()
