@@ -2245,10 +2245,10 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
 // It saves one launch's fixed cost per iteration (5.1 against 7.0 us per
 // iteration at 64^3, 9.9 against 12.5 at 128^3) but moves 41 B per unknown
 // against the pair's 34, which spill from L2 on larger systems (35.3 against
-// 32.1 us at 256^3).  Its rounding path differs from the pair's (solutions
-// about 4e-6 apart, equally far from the converged one on average), and in
-// the 64^3 sphere-drop replay its first step landed 7.8e-6 from the
-// converged pressure against the pair's 3.1e-6: the pair stays the default.
+// 32.1 us at 256^3).  Its carried recurrences (s = A p, w = A u) cost
+// accuracy on smooth systems: in the 64^3 sphere-drop replay both loops stop
+// at 100 iterations per step, and its pressure lands 4.6-6.7e-6 from the
+// converged one against the pair's 3.1e-6: the pair stays the default.
 bool use_cg1(const fsim_sim* s, int precision) {
   return precision == FSIM_PREC_FP32 && s->pcg_cg1 == 1;
 }
