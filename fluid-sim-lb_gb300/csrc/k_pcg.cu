@@ -1828,6 +1828,53 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1(const __grid_constan
   put_partials<DM, 3>(a, kPartCg1 + 3 * par, v);
 }
 
+// s = A p formed directly from p (in place, so the latest p_i), into the s
+// buffer that the next single-reduction launch reads (parity a.par): run
+// once per graph pass (and per host-polled chunk), it resets the drift that
+// the recurrence s_i = w_i + beta_i s_{i-1} accumulates in fp32.  A p is
+// summed in the reference's column order, as in the pair.
+template <typename T>
+__global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1_s(const __grid_constant__ PcgArgs a) {
+  __shared__ Tile<T> tiles[kHotThreads / 32];
+  __shared__ DiagInv<T> tab[16];
+  const T* p = static_cast<const T*>(a.p0);
+  T* sb = static_cast<T*>(a.sv[a.par]);
+  const int lane = threadIdx.x & 31;
+  const int wpb = kHotThreads / 32;
+  const int nhw = 2 * a.n_pleaf, hstride = gridDim.x * wpb;
+  int hw = blockIdx.x * wpb + (threadIdx.x >> 5);
+  fill_diag_table<T>(tab);
+  int nbl = hw < nhw ? face_slot_lane(a.nbr, hw >> 1, lane) : -1;
+  pdl_wait();
+  pdl_trigger();
+  __syncthreads();  // the diagonal table
+  Tile<T>& tile = tiles[threadIdx.x >> 5];
+  for (; hw < nhw; hw += hstride) {
+    const int nbl_next =
+        hw + hstride < nhw ? face_slot_lane(a.nbr, (hw + hstride) >> 1, lane) : -1;
+    int fs[6];
+    face_slots(nbl, fs);
+    nbl = nbl_next;
+    const HalfLeaf h = half_pos(hw, lane);
+    const unsigned o = unsigned(h.s) * 512u + unsigned(h.c);
+    const uint2 f = ldflags(a.flags, o);
+    Col<T> P, H;
+    ldcol(p, o, P);
+    int hslot, hvox;
+    halo_col(h, fs, hslot, hvox);
+    ldcol(p, slot_or_null(hslot, a.n_pleaf) * 512u + unsigned(hvox), H);
+    const T zm = ldv(p + (slot_or_null(fs[4], a.n_pleaf) * 512u + unsigned(h.c) + 7u));
+    const T zp = ldv(p + (slot_or_null(fs[5], a.n_pleaf) * 512u + unsigned(h.c)));
+    __syncwarp();
+    st_col_sh(tile, h.lx + 1, h.cy + 1, P);
+    if (h.lx != 2) st_col_sh(tile, h.tx, h.ty, H);
+    __syncwarp();
+    Col<T> ap;
+    stencil_col<T>(tile, tab, h.lx, h.cy, P, f, zm, zp, ap);
+    stcol(sb, o, ap);
+  }
+}
+
 // MIXED: x64 += d (inner solution); d is the fp32 x of the inner solve.
 __global__ void k_accumulate_x64(const __grid_constant__ PcgArgs a) {
   const int64_t n = int64_t(a.n_pleaf) * 512;
@@ -2020,7 +2067,7 @@ int pass_iters_for(const fsim_sim* s) {
 // of that kernel, one per iteration, alternating parity.
 template <typename T, int DM>
 int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pass_iters,
-                   void* fn_cg1 = nullptr) {
+                   void* fn_cg1 = nullptr, void* fn_fix = nullptr) {
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   cudaGraphConditionalHandle h = 0;
@@ -2040,17 +2087,18 @@ int run_graph_loop(fsim_sim* s, PcgArgs a, int wgrid, int par0, bool pdl, int pa
     ap[0].par = par0;
     ap[1].par = par0 ^ 1;
     cudaGraphNode_t prev = nullptr;
-    const int nodes = fn_cg1 ? pass_iters : 2 * pass_iters;
+    const int nodes = fn_cg1 ? pass_iters + (fn_fix ? 1 : 0) : 2 * pass_iters;
     for (int k = 0; k < nodes && e == cudaSuccess; ++k) {
       cudaGraphNodeParams kn = {};
       kn.type = cudaGraphNodeTypeKernel;
+      // the s re-forming node closes the pass with the next launch's parity, par0
       void* args[] = {&ap[fn_cg1 ? (k & 1) : ((k >> 1) & 1)]};
       kn.kernel.gridDim = dim3(unsigned(wgrid));
       kn.kernel.blockDim = dim3(unsigned(kHotThreads));
       kn.kernel.kernelParams = args;
       const bool zd = use_zdirect<T>(s, a.n_pleaf);
       if (fn_cg1) {
-        kn.kernel.func = fn_cg1;
+        kn.kernel.func = k == pass_iters ? fn_fix : fn_cg1;
         kn.kernel.sharedMemBytes = 0u;
       } else {
         kn.kernel.func = (k & 1) ? update_kernel<T, DM>(s, zd)
@@ -2191,6 +2239,7 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
   a.cond = 0;
   FSIM_LAUNCH(s, "pcg_setup", (k_pcg_setup<T, DM>), grid, kThreads, 0, a);
   void* const fn = reinterpret_cast<void*>(k_pcg_cg1<T, DM>);
+  void* const fn_fix = reinterpret_cast<void*>(k_pcg_cg1_s<T>);
   const int wpb = kHotThreads / 32;
   int occ = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kHotThreads, 0);
@@ -2205,25 +2254,28 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
     const int pass_iters = pass_iters_for(s);
     rc = FSIM_ERR_CUDA;
     if (s->use_pdl) {
-      rc = run_graph_loop<T, DM>(s, a, wgrid, 1, true, pass_iters, fn);
+      rc = run_graph_loop<T, DM>(s, a, wgrid, 1, true, pass_iters, fn, fn_fix);
       if (rc != FSIM_OK) s->use_pdl = false;
     }
-    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, 1, false, pass_iters, fn);
+    if (rc != FSIM_OK) rc = run_graph_loop<T, DM>(s, a, wgrid, 1, false, pass_iters, fn, fn_fix);
     if (rc == FSIM_OK) {
       lt.stop();
       FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                  s->stream));
       FSIM_CK(s, cudaStreamSynchronize(s->stream));
-      // one launch per iteration; the stop is set in the head of launch n
+      // one launch per iteration and one s re-forming launch per pass; the
+      // stop is set in the head of launch n
       const int64_t n = std::max(s->h_sc->iter, 0);
-      s->launches += pass_iters * (n / pass_iters + 1);
+      s->launches += (pass_iters + 1) * (n / pass_iters + 1);
       s->pcg_seg_max = std::max(s->pcg_seg_max, int(std::min<int64_t>(n, 1 << 30)));
       return FSIM_OK;
     }
     s->use_graphs = false;
   }
+  // host-polled: chunks of the graph's pass length, so that s is re-formed
+  // after the same iterations and the solve is bitwise the graph loop's
   a.cond = 0;
-  int chunk = 8;
+  const int chunk = pass_iters_for(s);
   int64_t launched = 1;
   LoopTimer lt(s);
   for (;;) {
@@ -2235,7 +2287,8 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
       a.par = int(launched & 1);
       if ((rc = launch_hot(s, "pcg_cg1", fn, wgrid, a)) != FSIM_OK) return rc;
     }
-    if (chunk < 64) chunk *= 2;
+    a.par = int(launched & 1);  // the next launch's s buffer
+    if ((rc = launch_hot(s, "pcg_cg1_s", fn_fix, wgrid, a)) != FSIM_OK) return rc;
   }
   lt.stop();
   return FSIM_OK;
