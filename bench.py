@@ -86,7 +86,7 @@ PCG_PAIRS = {"pcg_spmv": "pcg_update", "pcg_update": "pcg_spmv",
              "pcg_spmv_mixed": "pcg_update_mixed", "pcg_update_mixed": "pcg_spmv_mixed",
              "pcg_spmv_f64": "pcg_update_f64", "pcg_update_f64": "pcg_spmv_f64"}
 # Kernels that are a whole PCG iteration on their own.
-PCG_SINGLE = {"pcg_cg1"}
+PCG_SINGLE = {"pcg_cg1"}  # with its per-pass s re-forming (pcg_cg1_s), counted in loop_ms
 
 
 def peaks():

@@ -1614,7 +1614,8 @@ __global__ void __launch_bounds__(kHotThreads, 4)
 // owner's bits), which is why r, w and s alternate between two buffers by
 // launch parity, while x and p, read only at their own cells, are updated in
 // place.  The first launch of a solve (after setup) computes w_0 = A M r_0
-// with alpha = beta = 0 and w, s, p, x taken as 0.
+// with alpha = beta = 0 and w, s, p, x taken as 0.  s drifts from A p in
+// fp32 along its recurrence; k_pcg_cg1_s re-forms it once per pass.
 // Per unknown and iteration it reads flags, x, p, r, w, s and writes x, p, r,
 // w, s: 41 B, against the pair's 34 B.
 constexpr int kPartCg1 = 0;  // part[] rows: gamma, delta, r.r of launch parity 0, then of parity 1
@@ -2298,10 +2299,10 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
 // It saves one launch's fixed cost per iteration (5.1 against 7.0 us per
 // iteration at 64^3, 9.9 against 12.5 at 128^3) but moves 41 B per unknown
 // against the pair's 34, which spill from L2 on larger systems (35.3 against
-// 32.1 us at 256^3).  Its carried recurrences (s = A p, w = A u) cost
-// accuracy on smooth systems: in the 64^3 sphere-drop replay both loops stop
-// at 100 iterations per step, and its pressure lands 4.6-6.7e-6 from the
-// converged one against the pair's 3.1e-6: the pair stays the default.
+// 32.1 us at 256^3).  Its recurrence for s costs accuracy on smooth systems
+// even with s re-formed once per pass: on the first step of the 64^3
+// sphere-drop replay its pressure lands 1.22e-5 from the oracle's, against
+// the pair's 6.3e-6, so the pair stays the default.
 bool use_cg1(const fsim_sim* s, int precision) {
   return precision == FSIM_PREC_FP32 && s->pcg_cg1 == 1;
 }
