@@ -58,13 +58,17 @@ ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update
              "pcg_spmv_f64": 25, "pcg_update_f64": 41,
              # single-reduction iteration (FSIM_PCG_CG1=1): read flags, x, p, r, w, s;
              # write x, p, r, w, s
-             "pcg_cg1": 41}
+             "pcg_cg1": 41,
+             # resident loop: the pair's fused iteration (34 B per unknown when
+             # streamed); it keeps r, p and the flags on chip, so its own traffic is
+             # lower (x read and written, the r and p mirrors written: 16 B)
+             "pcg_resident": 34}
 # The same iteration in the textbook formulation, where z = M^-1 r and Ap are stored:
 #   Ap = A p and p.Ap:                read p, flags; write Ap                 =  9 B
 #   x += a p; r -= a Ap; z; r.r, r.z: read x, p, r, Ap, flags; write x, r, z  = 29 B
 #   p = z + b p:                      read z, p; write p                      = 12 B
 # (fp32 vectors), keyed by the spmv kernel of the pair.
-UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50, "pcg_cg1": 50}
+UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50, "pcg_cg1": 50, "pcg_resident": 50}
 # DRAM traffic per unknown per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
 # captures of `bench.py --pcg-micro`.  The fp32 pair: the 256^3 dam-break system (4,021,250
 # unknowns), host-launched loop (FSIM_PCG_GRAPH=0), caches NOT flushed between launches
@@ -86,7 +90,7 @@ PCG_PAIRS = {"pcg_spmv": "pcg_update", "pcg_update": "pcg_spmv",
              "pcg_spmv_mixed": "pcg_update_mixed", "pcg_update_mixed": "pcg_spmv_mixed",
              "pcg_spmv_f64": "pcg_update_f64", "pcg_update_f64": "pcg_spmv_f64"}
 # Kernels that are a whole PCG iteration on their own.
-PCG_SINGLE = {"pcg_cg1"}  # with its per-pass s re-forming (pcg_cg1_s), counted in loop_ms
+PCG_SINGLE = {"pcg_cg1", "pcg_resident"}  # pcg_cg1 with its per-pass s re-forming (pcg_cg1_s), in loop_ms
 
 
 def peaks():

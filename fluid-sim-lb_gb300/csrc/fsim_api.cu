@@ -262,6 +262,9 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
   // FSIM_PCG_CG1=1: fp32 solves by the single-reduction iteration (opt-in)
   if (const char* c = std::getenv("FSIM_PCG_CG1")) s->pcg_cg1 = c[0] == '1' ? 1 : 0;
+  // FSIM_PCG_RES=0/1: fp32 solves never / wherever it fits by the on-chip
+  // resident loop (default: by system size)
+  if (const char* c = std::getenv("FSIM_PCG_RES")) s->pcg_res = c[0] == '1' ? 1 : 0;
   for (int a = 0; a < 3; ++a) {
     s->lm.n[a] = cfg->global_dims[a];
     s->lm.lmax[a] = cfg->global_dims[a] / 8;

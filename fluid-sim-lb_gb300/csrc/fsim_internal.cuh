@@ -160,8 +160,9 @@ struct alignas(16) PcgScalars {
   double tol2_outer;  // MIXED: outer tolerance squared; a segment never stops below tol2_outer*bb
   unsigned int cnt_s, cnt_r;
   unsigned long long n_rows;  // FLUID cells (unknowns), counted by setup
-  // bulk-copy spmv: FSIM_ERR_TIMEOUT when a bounded stage wait gave up (0: none)
-  unsigned int wait_err, wait_pad[3];
+  // bulk-copy spmv: FSIM_ERR_TIMEOUT when a bounded stage wait gave up (0: none);
+  // resident loop: grid-barrier arrivals and its timeout flag
+  unsigned int wait_err, bar_count, bar_err, wait_pad;
   // hot-loop hand-off: [0] spmv -> update, [1] update -> spmv (and setup /
   // residual replacement -> spmv)
   PcgIterState st[2];
@@ -311,6 +312,10 @@ struct fsim_sim {
   // fp32 solves by the single-reduction (Chronopoulos-Gear) iteration, one
   // kernel per iteration (FSIM_PCG_CG1=1; opt-in)
   int pcg_cg1 = 0;
+  // fp32 solves by the resident loop (one persistent CTA per SM holding r, p
+  // and the flags on chip): -1 by system size, 0 never, 1 wherever it fits
+  // (FSIM_PCG_RES)
+  int pcg_res = -1;
 
   // water sources and the time they see
   std::vector<fsim_source> sources;

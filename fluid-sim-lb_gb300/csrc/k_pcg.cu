@@ -614,6 +614,19 @@ __device__ __forceinline__ void ld_col_sh(const Tile<T>& t, int x, int y, Col<T>
   }
 }
 
+// A z-column (8 cells) of a shared-memory array at float offset c (16-byte
+// aligned): two 16 B shared accesses.
+__device__ __forceinline__ void ld_col_box(const float* box, int c, Col<float>& col) {
+  const float4 u = *reinterpret_cast<const float4*>(box + c);
+  const float4 w = *reinterpret_cast<const float4*>(box + c + 4);
+  col.v[0] = u.x; col.v[1] = u.y; col.v[2] = u.z; col.v[3] = u.w;
+  col.v[4] = w.x; col.v[5] = w.y; col.v[6] = w.z; col.v[7] = w.w;
+}
+__device__ __forceinline__ void st_col_box(float* box, int c, const Col<float>& col) {
+  *reinterpret_cast<float4*>(box + c) = make_float4(col.v[0], col.v[1], col.v[2], col.v[3]);
+  *reinterpret_cast<float4*>(box + c + 4) = make_float4(col.v[4], col.v[5], col.v[6], col.v[7]);
+}
+
 // A p on the lane's column, summed in the reference's column order
 // (-x,-y,-z, diag, +z,+y,+x); 0 off-fluid.  The four x/y neighbour columns
 // come from the tile; zm / zp are the -z / +z face cells.
@@ -1876,6 +1889,355 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1_s(const __grid_const
   }
 }
 
+// ---- on-chip resident loop: one persistent CTA per SM ---------------------------
+// fp32 solves whose particle leaves fit on chip (FSIM_PCG_RES=1): one
+// cooperative launch runs every iteration.  CTA c owns the contiguous slots
+// [c * per, c * per + nl), per = ceil(n_pleaf / G) <= kResLeaves, and keeps
+// them resident: r in registers (each warp owns up to kResHL half leaves, a
+// lane one z-column of each), p and the flags in shared memory.  Per
+// iteration, as the reference's ComputeLocal1-3 (common/solver.cc:297-366):
+//   S: p = z + beta p on the own columns (into shared memory and a global
+//      mirror), then A p and the p.Ap partials;
+//   grid barrier: every CTA sums the G partials in CTA order -> alpha;
+//   U: A p again, x += alpha p (global), r -= alpha A p (registers, and a
+//      global mirror), the r.r and r.z partials;
+//   grid barrier -> r.r, r.z, beta and the loop test.
+// Stencil neighbours in the CTA's own leaves come from shared memory; those
+// in other CTAs' leaves from the mirrors, read through L2 (written in this
+// launch): in S the neighbour's p is formed from its r and previous p (the
+// owner's operations, so the owner's bits; p alternates between two mirror
+// buffers by iteration parity), in U it is read from the p mirror.  A p is
+// summed in the reference's column order.  The dot products are summed per
+// thread, per CTA and over CTAs in fixed orders: the solve is deterministic
+// (its per-thread order differs from the pair's, so the bits do too).
+// Barrier waits are bounded (kResPolls); a CTA that gives up sets bar_err and
+// every CTA leaves the loop (FSIM_ERR_TIMEOUT).
+constexpr int kResWarps = 16;
+constexpr int kResThreads = kResWarps * 32;
+constexpr int kResHL = 7;                             // half leaves per warp
+constexpr int kResLeaves = kResWarps * kResHL / 2;    // leaves per CTA
+constexpr size_t kResSmem = size_t(kResLeaves) * 512 * (sizeof(float) + 1);  // p, flags
+constexpr unsigned kResPolls = 1u << 22;  // about 2-4 s of L2 round trips
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// a column written by another CTA of this launch: through L2, not L1
+__device__ __forceinline__ void ldcol_l2(const float* p, unsigned o, Col<float>& c) {
+  const float4 u = __ldcg(reinterpret_cast<const float4*>(p + o));
+  const float4 w = __ldcg(reinterpret_cast<const float4*>(p + o + 4));
+  c.v[0] = u.x; c.v[1] = u.y; c.v[2] = u.z; c.v[3] = u.w;
+  c.v[4] = w.x; c.v[5] = w.y; c.v[6] = w.z; c.v[7] = w.w;
+}
+
+// Grid barrier of round `round` with the CTA's NV partials: publish, arrive
+// (a GPU-scope release add on one counter, after the CTA barrier that orders
+// the CTA's mirror stores first), wait with acquire loads until all G CTAs
+// of the round have arrived, then sum the G partials in CTA order (every CTA
+// the same totals).  Rows row0.. of the float partials; each phase type has
+// its own rows, which a CTA can only rewrite after every CTA has passed the
+// next barrier, and so has read them.  Waits are bounded: a CTA that gives
+// up sets bar_err, which the others also poll.  (Publishing each partial
+// beside the round number in one 64-bit word, polled by every CTA, measured
+// slower: 33.2 against 30.1 us per iteration at 256^3.)
+template <int NV>
+__device__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0, unsigned round,
+                         double (&tot)[NV], double* s_tot, int* s_ok) {
+  block_sum_p<float, NV, kResThreads>(v);  // its CTA barrier orders the CTA's stores first
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a.partf[(row0 + k) * a.maxb + blockIdx.x] = v[k];
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(&a.sc->bar_count) : "memory");
+    const unsigned target = round * gridDim.x;
+    unsigned polls = 0;
+    int ok = 1;
+    while (ld_acquire_gpu(&a.sc->bar_count) < target) {
+      if ((++polls & 255u) == 0u &&
+          (polls > kResPolls || ld_acquire_gpu(&a.sc->bar_err) != 0u)) {
+        ok = 0;
+        break;
+      }
+    }
+    if (!ok) atomicExch(&a.sc->bar_err, 1u);
+    *s_ok = ok;
+  }
+  __syncthreads();
+  if (!*s_ok) return false;
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      float x = 0.f;
+      for (int i = lane; i < int(gridDim.x); i += 32)
+        x = __fadd_rn(x, __ldcg(a.partf + (row0 + k) * a.maxb + i));
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = __fadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
+      if (lane == 0) s_tot[k] = double(x);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = s_tot[k];
+  return true;
+}
+
+// Where a neighbour of the CTA's cells lives.
+struct ResFrame {
+  const float* ps;       // shared p of the CTA's leaves
+  const uint8_t* fsm;    // shared flags
+  int L0, nl, n_pleaf;
+};
+__device__ __forceinline__ bool res_local(const ResFrame& fr, int slot) {
+  return slot >= fr.L0 && slot < fr.L0 + fr.nl;
+}
+
+// p (current iteration) of the column at cell offset v of leaf `slot`: from
+// shared memory for the CTA's leaves; else in S formed from the mirrors of
+// r and the previous p, in U read from the p mirror.
+template <bool U>
+__device__ __forceinline__ void res_pcol(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
+                                         const float* pm_new, const DiagInv<float>* tab, float beta,
+                                         int slot, int v, Col<float>& out) {
+  if (res_local(fr, slot)) {
+    ld_col_box(fr.ps, (slot - fr.L0) * 512 + v, out);
+  } else {
+    const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
+    if (U) {
+      ldcol_l2(pm_new, o, out);
+    } else {
+      Col<float> r, po;
+      ldcol_l2(static_cast<const float*>(a.r), o, r);
+      ldcol_l2(pm_old, o, po);
+      const uint2 f = ldflags(a.flags, o);
+#pragma unroll
+      for (int z = 0; z < 8; ++z) out.v[z] = pnew_of<float>(tab, fbyte(f, z), r.v[z], po.v[z], beta);
+    }
+  }
+}
+template <bool U>
+__device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
+                                           const float* pm_old, const float* pm_new,
+                                           const DiagInv<float>* tab, float beta, int slot, int v) {
+  if (res_local(fr, slot)) return fr.ps[(slot - fr.L0) * 512 + v];
+  const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
+  if (U) return __ldcg(pm_new + o);
+  return pnew_of<float>(tab, a.flags[o], __ldcg(static_cast<const float*>(a.r) + o),
+                        __ldcg(pm_old + o), beta);
+}
+
+// A p on the lane's column (x, y) of leaf s (own values P), in the
+// reference's column order; 0 off-fluid.
+template <bool U>
+__device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
+                                       const float* pm_new, const DiagInv<float>* tab, float beta,
+                                       int s, int x, int y, const int fs[6], const Col<float>& P,
+                                       uint2 f, Col<float>& ap) {
+  // one neighbour column at a time, in the reference's order: -x, -y, -z,
+  // diag, +z, +y, +x
+  Col<float> nc;
+#pragma unroll
+  for (int z = 0; z < 8; ++z) ap.v[z] = 0.f;
+  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, x > 0 ? s : fs[0],
+              (x > 0 ? x - 1 : 7) * 64 + y * 8, nc);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
+  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, y > 0 ? s : fs[2],
+              x * 64 + (y > 0 ? y - 1 : 7) * 8, nc);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
+  const float zm = res_pcell<U>(fr, a, pm_old, pm_new, tab, beta, fs[4], x * 64 + y * 8 + 7);
+  const float zp = res_pcell<U>(fr, a, pm_old, pm_new, tab, beta, fs[5], x * 64 + y * 8);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) {
+    const uint8_t g = fbyte(f, z);
+    const float vzm = z == 0 ? zm : P.v[(z + 7) & 7], vzp = z == 7 ? zp : P.v[(z + 1) & 7];
+    ap.v[z] = tsub(ap.v[z], vzm);
+    ap.v[z] = tadd(ap.v[z], tmul(tab[g & 15].d, P.v[z]));
+    ap.v[z] = tsub(ap.v[z], vzp);
+  }
+  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, y < 7 ? s : fs[3],
+              x * 64 + (y < 7 ? y + 1 : 0) * 8, nc);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
+  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, x < 7 ? s : fs[1],
+              (x < 7 ? x + 1 : 0) * 64 + y * 8, nc);
+#pragma unroll
+  for (int z = 0; z < 8; ++z) {
+    ap.v[z] = tsub(ap.v[z], nc.v[z]);
+    if (!(fbyte(f, z) & 1)) ap.v[z] = 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_constant__ PcgArgs a) {
+  extern __shared__ __align__(16) unsigned char res_smem[];
+  float* ps = reinterpret_cast<float*>(res_smem);
+  uint8_t* fsm = res_smem + size_t(kResLeaves) * 512 * sizeof(float);
+  __shared__ DiagInv<float> tab[16];
+  __shared__ double s_tot[2];
+  __shared__ int s_ok;
+  PcgScalars* sc = a.sc;
+  const int G = int(gridDim.x);
+  const int per = (a.n_pleaf + G - 1) / G;  // the host checks per <= kResLeaves
+  ResFrame fr;
+  fr.ps = ps;
+  fr.fsm = fsm;
+  fr.L0 = int(blockIdx.x) * per;
+  fr.nl = max(0, min(per, a.n_pleaf - fr.L0));
+  fr.n_pleaf = a.n_pleaf;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  fill_diag_table<float>(tab);
+  for (int i = threadIdx.x; i < fr.nl * 512; i += kResThreads) {
+    fsm[i] = a.flags[int64_t(fr.L0) * 512 + i];
+    ps[i] = 0.f;  // p of iteration -1
+  }
+  // the warp's half leaves: r into registers, the face slots
+  float rc[kResHL][8];
+  int nbl[kResHL];
+#pragma unroll
+  for (int k = 0; k < kResHL; ++k) {
+    const int hl = warp + k * kResWarps;
+    nbl[k] = -1;
+#pragma unroll
+    for (int z = 0; z < 8; ++z) rc[k][z] = 0.f;
+    if (hl < 2 * fr.nl) {
+      const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+      Col<float> r0;
+      ldcol(static_cast<const float*>(a.r), unsigned(h.s) * 512u + unsigned(h.c), r0);
+#pragma unroll
+      for (int z = 0; z < 8; ++z) rc[k][z] = r0.v[z];
+      nbl[k] = face_slot_lane(a.nbr, h.s, lane);
+    }
+  }
+  __syncthreads();
+  const bool fp32 = sc->fp32 != 0;
+  int it = sc->iter, done = sc->done, status = sc->status;
+  const int max_iter = sc->max_iter;
+  double rz = sc->rz, rr = sc->rr, beta = 0.0, alpha = 0.0, pAp = 0.0, rz_old = sc->rz_old;
+  unsigned round = 0;
+  bool ok = true;
+  float* x = static_cast<float*>(a.x);
+  float* rmir = static_cast<float*>(a.r);
+  while (!done) {
+    done = (it >= max_iter) || converged(sc, rr);  // PCGDriver::Solve's loop test
+    if (done) break;
+    float* pm_new = static_cast<float*>((it & 1) ? a.p1 : a.p0);
+    const float* pm_old = static_cast<const float*>((it & 1) ? a.p0 : a.p1);
+    const float fbeta = float(beta);
+    // S: p = z + beta p on the own columns
+#pragma unroll
+    for (int k = 0; k < kResHL; ++k) {
+      const int hl = warp + k * kResWarps;
+      if (hl < 2 * fr.nl) {
+        const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+        const int ol = (hl >> 1) * 512 + h.c;
+        Col<float> P;
+        ld_col_box(ps, ol, P);
+        const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
+#pragma unroll
+        for (int z = 0; z < 8; ++z) P.v[z] = pnew_of<float>(tab, fbyte(f, z), rc[k][z], P.v[z], fbeta);
+        st_col_box(ps, ol, P);
+        stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
+      }
+    }
+    __syncthreads();
+    Dot<0> dp;
+#pragma unroll
+    for (int k = 0; k < kResHL; ++k) {
+      const int hl = warp + k * kResWarps;
+      int fs[6];
+      face_slots(nbl[k], fs);
+      if (hl < 2 * fr.nl) {
+        const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+        const int ol = (hl >> 1) * 512 + h.c;
+        Col<float> P, ap;
+        ld_col_box(ps, ol, P);
+        const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
+        res_ap<false>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
+#pragma unroll
+        for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
+      }
+    }
+    {
+      float v[1] = {dp.pvalue()};
+      double tot[1];
+      if (!(ok = res_sync<1>(a, v, 0, ++round, tot, s_tot, &s_ok))) break;
+      pAp = round_t(sc, tot[0]);
+      alpha = fp32 ? double(__fdiv_rn(float(rz), float(pAp))) : rz / pAp;
+      if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
+        status = FSIM_ERR_BREAKDOWN;
+        done = 1;
+        break;
+      }
+    }
+    // U: x += alpha p, r -= alpha A p
+    const float fa = float(alpha), fna = -fa;
+    Dot<0> drr, drz;
+#pragma unroll
+    for (int k = 0; k < kResHL; ++k) {
+      const int hl = warp + k * kResWarps;
+      int fs[6];
+      face_slots(nbl[k], fs);
+      if (hl < 2 * fr.nl) {
+        const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+        const int ol = (hl >> 1) * 512 + h.c;
+        const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
+        Col<float> P, ap;
+        ld_col_box(ps, ol, P);
+        const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
+        {
+          Col<float> X;
+          ldcol(x, og, X);
+#pragma unroll
+          for (int z = 0; z < 8; ++z) X.v[z] = tadd(tmul(fa, P.v[z]), X.v[z]);
+          stcol(x, og, X);
+        }
+        res_ap<true>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
+#pragma unroll
+        for (int z = 0; z < 8; ++z) {
+          const uint8_t g = fbyte(f, z);
+          rc[k][z] = tadd(tmul(fna, ap.v[z]), rc[k][z]);
+          drr.add(rc[k][z], rc[k][z]);
+          drz.add(rc[k][z], tmul(tab[g & 15].inv, rc[k][z]));
+          ap.v[z] = rc[k][z];
+        }
+        stcol(rmir, og, ap);
+      }
+    }
+    {
+      float v[2] = {drr.pvalue(), drz.pvalue()};
+      double tot[2];
+      if (!(ok = res_sync<2>(a, v, 1, ++round, tot, s_tot, &s_ok))) break;
+      rr = round_t(sc, tot[0]);
+      const double rzn = round_t(sc, tot[1]);
+      beta = fp32 ? double(__fdiv_rn(float(rzn), float(rz))) : rzn / rz;
+      rz_old = rz;
+      rz = rzn;
+      ++it;
+      if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
+        status = FSIM_ERR_BREAKDOWN;
+        done = 1;
+      }
+    }
+  }
+  if (!ok) {
+    status = FSIM_ERR_TIMEOUT;
+    done = 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc->iter = it;
+    sc->done = 1;
+    sc->status = status;
+    sc->rr = rr;
+    sc->rz = rz;
+    sc->rz_old = rz_old;
+    sc->alpha = alpha;
+    sc->beta = beta;
+    sc->pAp = pAp;
+  }
+}
+
 // MIXED: x64 += d (inner solution); d is the fp32 x of the inner solve.
 __global__ void k_accumulate_x64(const __grid_constant__ PcgArgs a) {
   const int64_t n = int64_t(a.n_pleaf) * 512;
@@ -2295,6 +2657,51 @@ int run_cg1(fsim_sim* s, PcgArgs& a, int grid) {
   return FSIM_OK;
 }
 
+// One fp32 solve by the resident loop: setup, then one cooperative launch of
+// one CTA per SM that runs every iteration.  FSIM_ERR_CUDA when the launch is
+// refused (the caller then runs the pair).
+int run_resident(fsim_sim* s, PcgArgs& a, int grid) {
+  void* const fn = reinterpret_cast<void*>(k_pcg_resident);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kResSmem)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return FSIM_ERR_CUDA;
+  }
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kResThreads, kResSmem);
+  if (occ < 1) return FSIM_ERR_CUDA;
+  a.cond = 0;
+  FSIM_LAUNCH(s, "pcg_setup", (k_pcg_setup<float, 0>), grid, kThreads, 0, a);
+  LoopTimer lt(s);
+  {
+    fsim::ProfScope ps(s, "pcg_resident");
+    void* args[] = {&a};
+    const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(unsigned(s->num_sms)),
+                                                      dim3(unsigned(kResThreads)), args, kResSmem,
+                                                      s->stream);
+    s->launches++;
+    if (e != cudaSuccess) return cuda_fail(s, e, "pcg_resident");
+  }
+  lt.stop();
+  FSIM_CK(s, cudaMemcpyAsync(s->h_sc, a.sc, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+  FSIM_CK(s, cudaStreamSynchronize(s->stream));
+  if (s->h_sc->bar_err) return fail(s, FSIM_ERR_TIMEOUT, "PCG: a resident-loop barrier gave up");
+  return FSIM_OK;
+}
+// The resident loop takes fp32 solves whose particle leaves fit (at most
+// kResLeaves per SM) and are many enough to amortise its two grid barriers
+// per iteration (about 4 us each): from kResMinLeaves per SM.  Measured per
+// iteration against the pair: 29.9 against 32.1 us at 256^3 (55 leaves per
+// SM), 12.5 against 12.5 at 128^3, 10.9 against 6.5-7.0 at 64^3 (about one
+// leaf per SM).  FSIM_PCG_RES=0 / 1 turns it off / on wherever it fits.
+constexpr int kResMinLeaves = 16;
+bool use_resident(const fsim_sim* s, int precision) {
+  if (precision != FSIM_PREC_FP32 || s->pcg_res == 0) return false;
+  const int64_t n = s->n_pleaf, sms = s->num_sms;
+  if (n > int64_t(kResLeaves) * sms) return false;
+  return s->pcg_res > 0 || n >= int64_t(kResMinLeaves) * sms;
+}
+
 // fp32 solves take the single-reduction iteration on request (FSIM_PCG_CG1=1).
 // It saves one launch's fixed cost per iteration (5.1 against 7.0 us per
 // iteration at 64^3, 9.9 against 12.5 at 128^3) but moves 41 B per unknown
@@ -2388,7 +2795,17 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
     *s->h_sc = h;
     FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
                                s->stream));
-    if (use_cg1(s, prm->precision)) {
+    if (use_resident(s, prm->precision)) {
+      rc = run_resident(s, a, grid);
+      if (rc == FSIM_ERR_CUDA) {  // cooperative launch refused: the pair
+        cudaGetLastError();
+        s->pcg_res = 0;
+        *s->h_sc = h;
+        FSIM_CK(s, cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(PcgScalars), cudaMemcpyHostToDevice,
+                                   s->stream));
+        rc = run_inner<float, 0>(s, a, grid, "pcg_setup", "pcg_spmv", "pcg_update");
+      }
+    } else if (use_cg1(s, prm->precision)) {
       for (int b = 0; b < 2; ++b) {
         a.w[b] = s->cgw[b];
         a.sv[b] = s->cgs[b];

@@ -14,10 +14,10 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(autouse=True)
 def _pair_loop(monkeypatch):
-    """These tests cover the spmv / update pair: fp32 solves of systems this
-    small would otherwise take the single-reduction loop
-    (tests/test_gpu_pcg_cg1.py)."""
+    """These tests cover the spmv / update pair, whatever the opt-in loops
+    (tests/test_gpu_pcg_cg1.py, tests/test_gpu_pcg_resident.py) would pick."""
     monkeypatch.setenv("FSIM_PCG_CG1", "0")
+    monkeypatch.setenv("FSIM_PCG_RES", "0")
 
 
 def _prepared(n=32, scene="dam_break", noise=True):
