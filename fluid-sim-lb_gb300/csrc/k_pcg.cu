@@ -1983,6 +1983,29 @@ __device__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0, unsigned ro
   return true;
 }
 
+// Shared p of the CTA's leaves in 16-byte chunk planes: float4 element
+// ((leaf * 2 + chunk) * 8 + x) * 8 + y holds the cells z = 4 chunk ..
+// 4 chunk + 3 of column (x, y), so the lanes of a quarter warp (consecutive
+// y) touch consecutive 16-byte words.  v is a cell offset x*64 + y*8 + z.
+__device__ __forceinline__ int ps_chunk(int leaf, int v, int chunk) {
+  return ((leaf * 2 + chunk) * 8 + (v >> 6)) * 8 + ((v >> 3) & 7);
+}
+__device__ __forceinline__ void ps_ldcol(const float* ps, int leaf, int v, Col<float>& c) {
+  const float4* q = reinterpret_cast<const float4*>(ps);
+  const float4 u = q[ps_chunk(leaf, v, 0)], w = q[ps_chunk(leaf, v, 1)];
+  c.v[0] = u.x; c.v[1] = u.y; c.v[2] = u.z; c.v[3] = u.w;
+  c.v[4] = w.x; c.v[5] = w.y; c.v[6] = w.z; c.v[7] = w.w;
+}
+__device__ __forceinline__ void ps_stcol(float* ps, int leaf, int v, const Col<float>& c) {
+  float4* q = reinterpret_cast<float4*>(ps);
+  q[ps_chunk(leaf, v, 0)] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
+  q[ps_chunk(leaf, v, 1)] = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
+}
+__device__ __forceinline__ float ps_cell(const float* ps, int leaf, int v) {
+  const int z = v & 7;
+  return ps[ps_chunk(leaf, v, z >> 2) * 4 + (z & 3)];
+}
+
 // Where a neighbour of the CTA's cells lives.
 struct ResFrame {
   const float* ps;       // shared p of the CTA's leaves
@@ -2001,7 +2024,7 @@ __device__ __forceinline__ void res_pcol(const ResFrame& fr, const PcgArgs& a, c
                                          const float* pm_new, const DiagInv<float>* tab, float beta,
                                          int slot, int v, Col<float>& out) {
   if (res_local(fr, slot)) {
-    ld_col_box(fr.ps, (slot - fr.L0) * 512 + v, out);
+    ps_ldcol(fr.ps, slot - fr.L0, v, out);
   } else {
     const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
     if (U) {
@@ -2020,7 +2043,7 @@ template <bool U>
 __device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
                                            const float* pm_old, const float* pm_new,
                                            const DiagInv<float>* tab, float beta, int slot, int v) {
-  if (res_local(fr, slot)) return fr.ps[(slot - fr.L0) * 512 + v];
+  if (res_local(fr, slot)) return ps_cell(fr.ps, slot - fr.L0, v);
   const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
   if (U) return __ldcg(pm_new + o);
   return pnew_of<float>(tab, a.flags[o], __ldcg(static_cast<const float*>(a.r) + o),
@@ -2133,11 +2156,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
         const int ol = (hl >> 1) * 512 + h.c;
         Col<float> P;
-        ld_col_box(ps, ol, P);
+        ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
 #pragma unroll
         for (int z = 0; z < 8; ++z) P.v[z] = pnew_of<float>(tab, fbyte(f, z), rc[k][z], P.v[z], fbeta);
-        st_col_box(ps, ol, P);
+        ps_stcol(ps, hl >> 1, h.c, P);
         stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
       }
     }
@@ -2152,7 +2175,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
         const int ol = (hl >> 1) * 512 + h.c;
         Col<float> P, ap;
-        ld_col_box(ps, ol, P);
+        ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
         res_ap<false>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
 #pragma unroll
@@ -2184,7 +2207,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         const int ol = (hl >> 1) * 512 + h.c;
         const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
         Col<float> P, ap;
-        ld_col_box(ps, ol, P);
+        ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
         {
           Col<float> X;
