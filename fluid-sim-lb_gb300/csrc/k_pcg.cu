@@ -1912,9 +1912,9 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1_s(const __grid_const
 // (its per-thread order differs from the pair's, so the bits do too).
 // Barrier waits are bounded (kResPolls); a CTA that gives up sets bar_err and
 // every CTA leaves the loop (FSIM_ERR_TIMEOUT).
-constexpr int kResWarps = 16;
+constexpr int kResWarps = 28;
 constexpr int kResThreads = kResWarps * 32;
-constexpr int kResHL = 7;                             // half leaves per warp
+constexpr int kResHL = 4;                             // half leaves per warp
 constexpr int kResLeaves = kResWarps * kResHL / 2;    // leaves per CTA
 constexpr size_t kResSmem = size_t(kResLeaves) * 512 * (sizeof(float) + 1);  // p, flags
 constexpr unsigned kResPolls = 1u << 22;  // about 2-4 s of L2 round trips
@@ -2093,6 +2093,30 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
   }
 }
 
+// r of the CTA's cells lives in tensor memory (TMEM): 256 columns allocated
+// by warp 0; warp w uses TMEM lanes 32 (w % 4) .. + 31 (the quarter it may
+// access) and columns (w / 4) * 32 + 8 k .. + 7 for its half leaf k (lane L
+// holds its column's 8 cells).  That leaves the registers to 28 warps.
+constexpr unsigned kResTmemCols = 256;
+static_assert((kResWarps + 3) / 4 * kResHL * 8 <= int(kResTmemCols), "TMEM columns");
+__device__ __forceinline__ void tmem_ld8(unsigned t, float (&v)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
+                 "=f"(v[6]), "=f"(v[7])
+               : "r"(t)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void tmem_st8(unsigned t, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n" ::"r"(t),
+               "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]),
+               "f"(v[7])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+}
+
 __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_constant__ PcgArgs a) {
   extern __shared__ __align__(16) unsigned char res_smem[];
   float* ps = reinterpret_cast<float*>(res_smem);
@@ -2100,6 +2124,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   __shared__ DiagInv<float> tab[16];
   __shared__ double s_tot[2];
   __shared__ int s_ok;
+  __shared__ unsigned s_taddr;
   PcgScalars* sc = a.sc;
   const int G = int(gridDim.x);
   const int per = (a.n_pleaf + G - 1) / G;  // the host checks per <= kResLeaves
@@ -2115,24 +2140,32 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     fsm[i] = a.flags[int64_t(fr.L0) * 512 + i];
     ps[i] = 0.f;  // p of iteration -1
   }
-  // the warp's half leaves: r into registers, the face slots
-  float rc[kResHL][8];
+  if (warp == 0) {
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(&s_taddr));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(sa),
+                 "r"(kResTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const unsigned tbase = s_taddr + ((32u * unsigned(warp & 3)) << 16) + unsigned(warp >> 2) * 32u;
+  // the warp's half leaves: r into TMEM, the face slots
   int nbl[kResHL];
 #pragma unroll
   for (int k = 0; k < kResHL; ++k) {
     const int hl = warp + k * kResWarps;
     nbl[k] = -1;
-#pragma unroll
-    for (int z = 0; z < 8; ++z) rc[k][z] = 0.f;
     if (hl < 2 * fr.nl) {
       const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
       Col<float> r0;
       ldcol(static_cast<const float*>(a.r), unsigned(h.s) * 512u + unsigned(h.c), r0);
-#pragma unroll
-      for (int z = 0; z < 8; ++z) rc[k][z] = r0.v[z];
+      tmem_st8(tbase + 8u * k, r0.v);
       nbl[k] = face_slot_lane(a.nbr, h.s, lane);
     }
   }
+  tmem_wait_st();
   __syncthreads();
   const bool fp32 = sc->fp32 != 0;
   int it = sc->iter, done = sc->done, status = sc->status;
@@ -2158,8 +2191,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         Col<float> P;
         ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
+        float rk[8];
+        tmem_ld8(tbase + 8u * k, rk);
 #pragma unroll
-        for (int z = 0; z < 8; ++z) P.v[z] = pnew_of<float>(tab, fbyte(f, z), rc[k][z], P.v[z], fbeta);
+        for (int z = 0; z < 8; ++z) P.v[z] = pnew_of<float>(tab, fbyte(f, z), rk[z], P.v[z], fbeta);
         ps_stcol(ps, hl >> 1, h.c, P);
         stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
       }
@@ -2217,17 +2252,21 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
           stcol(x, og, X);
         }
         res_ap<true>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
+        float rk[8];
+        tmem_ld8(tbase + 8u * k, rk);
 #pragma unroll
         for (int z = 0; z < 8; ++z) {
           const uint8_t g = fbyte(f, z);
-          rc[k][z] = tadd(tmul(fna, ap.v[z]), rc[k][z]);
-          drr.add(rc[k][z], rc[k][z]);
-          drz.add(rc[k][z], tmul(tab[g & 15].inv, rc[k][z]));
-          ap.v[z] = rc[k][z];
+          rk[z] = tadd(tmul(fna, ap.v[z]), rk[z]);
+          drr.add(rk[z], rk[z]);
+          drz.add(rk[z], tmul(tab[g & 15].inv, rk[z]));
+          ap.v[z] = rk[z];
         }
+        tmem_st8(tbase + 8u * k, rk);
         stcol(rmir, og, ap);
       }
     }
+    tmem_wait_st();
     {
       float v[2] = {drr.pvalue(), drz.pvalue()};
       double tot[2];
@@ -2247,6 +2286,16 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   if (!ok) {
     status = FSIM_ERR_TIMEOUT;
     done = 1;
+  }
+  // every warp is done with TMEM; warp 0 frees it
+  tmem_wait_st();
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(s_taddr),
+                 "r"(kResTmemCols)
+                 : "memory");
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     sc->iter = it;
