@@ -2093,12 +2093,15 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
   }
 }
 
-// r of the CTA's cells lives in tensor memory (TMEM): 256 columns allocated
-// by warp 0; warp w uses TMEM lanes 32 (w % 4) .. + 31 (the quarter it may
-// access) and columns (w / 4) * 32 + 8 k .. + 7 for its half leaf k (lane L
-// holds its column's 8 cells).  That leaves the registers to 28 warps.
-constexpr unsigned kResTmemCols = 256;
-static_assert((kResWarps + 3) / 4 * kResHL * 8 <= int(kResTmemCols), "TMEM columns");
+// r and x of the CTA's cells live in tensor memory (TMEM): all 512 columns,
+// allocated by warp 0; warp w uses TMEM lanes 32 (w % 4) .. + 31 (the
+// quarter it may access), and for its half leaf k columns (w / 4) * 32 + 8 k
+// .. + 7 for r and the same + kResTmemX for x (lane L holds its column's 8
+// cells).  That leaves the registers to 28 warps, and x is read and written
+// in global memory once per solve.
+constexpr unsigned kResTmemCols = 512;
+constexpr unsigned kResTmemX = 256;
+static_assert((kResWarps + 3) / 4 * kResHL * 8 <= int(kResTmemX), "TMEM columns");
 __device__ __forceinline__ void tmem_ld8(unsigned t, float (&v)[8]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
                : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
@@ -2151,7 +2154,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const unsigned tbase = s_taddr + ((32u * unsigned(warp & 3)) << 16) + unsigned(warp >> 2) * 32u;
-  // the warp's half leaves: r into TMEM, the face slots
+  // the warp's half leaves: r and x into TMEM, the face slots
   int nbl[kResHL];
 #pragma unroll
   for (int k = 0; k < kResHL; ++k) {
@@ -2159,9 +2162,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     nbl[k] = -1;
     if (hl < 2 * fr.nl) {
       const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+      const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
       Col<float> r0;
-      ldcol(static_cast<const float*>(a.r), unsigned(h.s) * 512u + unsigned(h.c), r0);
+      ldcol(static_cast<const float*>(a.r), og, r0);
       tmem_st8(tbase + 8u * k, r0.v);
+      ldcol(static_cast<const float*>(a.x), og, r0);
+      tmem_st8(tbase + kResTmemX + 8u * k, r0.v);
       nbl[k] = face_slot_lane(a.nbr, h.s, lane);
     }
   }
@@ -2245,11 +2251,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
         {
-          Col<float> X;
-          ldcol(x, og, X);
+          float X[8];
+          tmem_ld8(tbase + kResTmemX + 8u * k, X);
 #pragma unroll
-          for (int z = 0; z < 8; ++z) X.v[z] = tadd(tmul(fa, P.v[z]), X.v[z]);
-          stcol(x, og, X);
+          for (int z = 0; z < 8; ++z) X[z] = tadd(tmul(fa, P.v[z]), X[z]);
+          tmem_st8(tbase + kResTmemX + 8u * k, X);
         }
         res_ap<true>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
         float rk[8];
@@ -2287,8 +2293,19 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     status = FSIM_ERR_TIMEOUT;
     done = 1;
   }
-  // every warp is done with TMEM; warp 0 frees it
+  // x back to global memory; every warp is then done with TMEM, and warp 0
+  // frees it
   tmem_wait_st();
+#pragma unroll
+  for (int k = 0; k < kResHL; ++k) {
+    const int hl = warp + k * kResWarps;
+    if (hl < 2 * fr.nl) {
+      const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+      Col<float> X;
+      tmem_ld8(tbase + kResTmemX + 8u * k, X.v);
+      stcol(x, unsigned(h.s) * 512u + unsigned(h.c), X);
+    }
+  }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   if (warp == 0) {
