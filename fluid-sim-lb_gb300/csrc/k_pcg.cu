@@ -1966,15 +1966,31 @@ __device__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0, unsigned ro
   __syncthreads();
   if (!*s_ok) return false;
   if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
+    // lane adds partials lane, lane + 32, ... in that order; each batch's
+    // loads are all issued before its adds (a zero pad adds exactly nothing)
+    const int lane = threadIdx.x, G = int(gridDim.x);
+    float x[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) x[k] = 0.f;
+    for (int i0 = lane; i0 < G; i0 += 32 * 8) {
+      float t[NV][8];
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int i = i0 + 32 * u;
+          t[k][u] = i < G ? __ldcg(a.partf + (row0 + k) * a.maxb + i) : 0.f;
+        }
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) x[k] = __fadd_rn(x[k], t[k][u]);
+    }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-      float x = 0.f;
-      for (int i = lane; i < int(gridDim.x); i += 32)
-        x = __fadd_rn(x, __ldcg(a.partf + (row0 + k) * a.maxb + i));
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x = __fadd_rn(x, __shfl_down_sync(0xffffffffu, x, o));
-      if (lane == 0) s_tot[k] = double(x);
+      for (int o = 16; o > 0; o >>= 1) x[k] = __fadd_rn(x[k], __shfl_down_sync(0xffffffffu, x[k], o));
+      if (lane == 0) s_tot[k] = double(x[k]);
     }
   }
   __syncthreads();
