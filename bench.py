@@ -60,8 +60,8 @@ ALG_BYTES = {"pcg_spmv": 13, "pcg_update": 21, "pcg_spmv_mixed": 13, "pcg_update
              # write x, p, r, w, s
              "pcg_cg1": 41,
              # resident loop: the pair's fused iteration (34 B per unknown when
-             # streamed); it keeps r, p and the flags on chip, so its own traffic is
-             # lower (x read and written, the r and p mirrors written: 16 B)
+             # streamed); it keeps x, r, p and the flags on chip, so its own traffic
+             # is lower (the r and p mirrors written, 8 B, and the remote halo read)
              "pcg_resident": 34}
 # The same iteration in the textbook formulation, where z = M^-1 r and Ap are stored:
 #   Ap = A p and p.Ap:                read p, flags; write Ap                 =  9 B
@@ -420,7 +420,8 @@ def roofline(res):
         loop = sum(lms)
         achieved = tot_bytes / (loop * 1e-3) / 1e9
         n_rows = float(np.mean(rws))
-        out.update(kernel="pcg_iteration (" + " + ".join(names) + ", graph loop)",
+        loop_form = "one cooperative launch per solve" if name == "pcg_resident" else "graph loop"
+        out.update(kernel="pcg_iteration (" + " + ".join(names) + ", " + loop_form + ")",
                    achieved=achieved, frac=achieved / peak, alg_bytes_per_unknown=per,
                    alg_bytes_per_launch=per * n_rows, unknowns=n_rows,
                    us_per_iteration=loop * 1e3 / max(sum(its), 1), working_launches=sum(its),

@@ -309,17 +309,32 @@ struct PcgArgs {
   void* sv[2];      // single-reduction CG: s = A p (by parity)
 };
 
-__device__ __forceinline__ bool converged(const PcgScalars* sc, double rr) {
-  if (sc->mode == FSIM_PCG_FIXED) return false;
-  if (sc->mode == FSIM_PCG_ABSOLUTE) {
-    if (sc->fp32) return float(rr) < float(sc->thr);
-    return rr < sc->thr;
-  }
-  return rr <= sc->thr;
+// The loop test and the rounding of a total to the vectors' type, from the
+// solve's settings (mode, fp32, threshold).
+struct PcgRule {
+  int mode;
+  bool fp32;
+  double thr;
+};
+__device__ __forceinline__ PcgRule pcg_rule(const PcgScalars* sc) {
+  return PcgRule{sc->mode, sc->fp32 != 0, sc->thr};
 }
-
+__device__ __forceinline__ bool converged(const PcgRule& q, double rr) {
+  if (q.mode == FSIM_PCG_FIXED) return false;
+  if (q.mode == FSIM_PCG_ABSOLUTE) {
+    if (q.fp32) return float(rr) < float(q.thr);
+    return rr < q.thr;
+  }
+  return rr <= q.thr;
+}
+__device__ __forceinline__ double round_t(const PcgRule& q, double v) {
+  return q.fp32 ? double(float(v)) : v;
+}
+__device__ __forceinline__ bool converged(const PcgScalars* sc, double rr) {
+  return converged(pcg_rule(sc), rr);
+}
 __device__ __forceinline__ double round_t(const PcgScalars* sc, double v) {
-  return sc->fp32 ? double(float(v)) : v;
+  return round_t(pcg_rule(sc), v);
 }
 
 // Flags from the marker, r = b (or keep), x = 0, and r.r, r.z, b.b.
@@ -1936,15 +1951,16 @@ __device__ __forceinline__ void ldcol_l2(const float* p, unsigned o, Col<float>&
 // (a GPU-scope release add on one counter, after the CTA barrier that orders
 // the CTA's mirror stores first), wait with acquire loads until all G CTAs
 // of the round have arrived, then sum the G partials in CTA order (every CTA
-// the same totals).  Rows row0.. of the float partials; each phase type has
+// the same totals), and thread 0 runs fin(totals) before the closing CTA
+// barrier.  Rows row0.. of the float partials; each phase type has
 // its own rows, which a CTA can only rewrite after every CTA has passed the
 // next barrier, and so has read them.  Waits are bounded: a CTA that gives
 // up sets bar_err, which the others also poll.  (Publishing each partial
 // beside the round number in one 64-bit word, polled by every CTA, measured
 // slower: 33.2 against 30.1 us per iteration at 256^3.)
-template <int NV>
-__device__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0, unsigned round,
-                         double (&tot)[NV], double* s_tot, int* s_ok) {
+template <int NV, typename F>
+__device__ __forceinline__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0,
+                                         unsigned round, int* s_ok, F&& fin) {
   block_sum_p<float, NV, kResThreads>(v);  // its CTA barrier orders the CTA's stores first
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -1986,16 +2002,16 @@ __device__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0, unsigned ro
 #pragma unroll
         for (int u = 0; u < 8; ++u) x[k] = __fadd_rn(x[k], t[k][u]);
     }
+    double tot[NV];
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x[k] = __fadd_rn(x[k], __shfl_down_sync(0xffffffffu, x[k], o));
-      if (lane == 0) s_tot[k] = double(x[k]);
+      tot[k] = double(x[k]);
     }
+    if (lane == 0) fin(tot);
   }
   __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = s_tot[k];
   return true;
 }
 
@@ -2022,6 +2038,13 @@ __device__ __forceinline__ float ps_cell(const float* ps, int leaf, int v) {
   return ps[ps_chunk(leaf, v, z >> 2) * 4 + (z & 3)];
 }
 
+// The resident loop's scalar state, kept by thread 0.
+struct ResScalars {
+  double rr, rz, rz_old, alpha, beta, pAp;
+  int status, max_iter;
+  PcgRule rule;
+};
+
 // Where a neighbour of the CTA's cells lives.
 struct ResFrame {
   const float* ps;       // shared p of the CTA's leaves
@@ -2033,61 +2056,53 @@ __device__ __forceinline__ bool res_local(const ResFrame& fr, int slot) {
 }
 
 // p (current iteration) of the column at cell offset v of leaf `slot`: from
-// shared memory for the CTA's leaves; else in S formed from the mirrors of
-// r and the previous p, in U read from the p mirror.
-template <bool U>
+// shared memory for the CTA's leaves; else formed from the mirrors of r and
+// the previous p (the owner's operations, so the owner's bits).
 __device__ __forceinline__ void res_pcol(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
-                                         const float* pm_new, const DiagInv<float>* tab, float beta,
-                                         int slot, int v, Col<float>& out) {
+                                         const DiagInv<float>* tab, float beta, int slot, int v,
+                                         Col<float>& out) {
   if (res_local(fr, slot)) {
     ps_ldcol(fr.ps, slot - fr.L0, v, out);
   } else {
     const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
-    if (U) {
-      ldcol_l2(pm_new, o, out);
-    } else {
-      Col<float> r, po;
-      ldcol_l2(static_cast<const float*>(a.r), o, r);
-      ldcol_l2(pm_old, o, po);
-      const uint2 f = ldflags(a.flags, o);
+    Col<float> r, po;
+    ldcol_l2(static_cast<const float*>(a.r), o, r);
+    ldcol_l2(pm_old, o, po);
+    const uint2 f = ldflags(a.flags, o);
 #pragma unroll
-      for (int z = 0; z < 8; ++z) out.v[z] = pnew_of<float>(tab, fbyte(f, z), r.v[z], po.v[z], beta);
-    }
+    for (int z = 0; z < 8; ++z) out.v[z] = pnew_of<float>(tab, fbyte(f, z), r.v[z], po.v[z], beta);
   }
 }
-template <bool U>
 __device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
-                                           const float* pm_old, const float* pm_new,
-                                           const DiagInv<float>* tab, float beta, int slot, int v) {
+                                           const float* pm_old, const DiagInv<float>* tab,
+                                           float beta, int slot, int v) {
   if (res_local(fr, slot)) return ps_cell(fr.ps, slot - fr.L0, v);
   const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
-  if (U) return __ldcg(pm_new + o);
   return pnew_of<float>(tab, a.flags[o], __ldcg(static_cast<const float*>(a.r) + o),
                         __ldcg(pm_old + o), beta);
 }
 
 // A p on the lane's column (x, y) of leaf s (own values P), in the
 // reference's column order; 0 off-fluid.
-template <bool U>
 __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
-                                       const float* pm_new, const DiagInv<float>* tab, float beta,
-                                       int s, int x, int y, const int fs[6], const Col<float>& P,
-                                       uint2 f, Col<float>& ap) {
+                                       const DiagInv<float>* tab, float beta, int s, int x, int y,
+                                       const int fs[6], const Col<float>& P, uint2 f,
+                                       Col<float>& ap) {
   // one neighbour column at a time, in the reference's order: -x, -y, -z,
   // diag, +z, +y, +x
   Col<float> nc;
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = 0.f;
-  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, x > 0 ? s : fs[0],
+  res_pcol(fr, a, pm_old, tab, beta, x > 0 ? s : fs[0],
               (x > 0 ? x - 1 : 7) * 64 + y * 8, nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
-  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, y > 0 ? s : fs[2],
+  res_pcol(fr, a, pm_old, tab, beta, y > 0 ? s : fs[2],
               x * 64 + (y > 0 ? y - 1 : 7) * 8, nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
-  const float zm = res_pcell<U>(fr, a, pm_old, pm_new, tab, beta, fs[4], x * 64 + y * 8 + 7);
-  const float zp = res_pcell<U>(fr, a, pm_old, pm_new, tab, beta, fs[5], x * 64 + y * 8);
+  const float zm = res_pcell(fr, a, pm_old, tab, beta, fs[4], x * 64 + y * 8 + 7);
+  const float zp = res_pcell(fr, a, pm_old, tab, beta, fs[5], x * 64 + y * 8);
 #pragma unroll
   for (int z = 0; z < 8; ++z) {
     const uint8_t g = fbyte(f, z);
@@ -2096,11 +2111,11 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
     ap.v[z] = tadd(ap.v[z], tmul(tab[g & 15].d, P.v[z]));
     ap.v[z] = tsub(ap.v[z], vzp);
   }
-  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, y < 7 ? s : fs[3],
+  res_pcol(fr, a, pm_old, tab, beta, y < 7 ? s : fs[3],
               x * 64 + (y < 7 ? y + 1 : 0) * 8, nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
-  res_pcol<U>(fr, a, pm_old, pm_new, tab, beta, x < 7 ? s : fs[1],
+  res_pcol(fr, a, pm_old, tab, beta, x < 7 ? s : fs[1],
               (x < 7 ? x + 1 : 0) * 64 + y * 8, nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) {
@@ -2109,15 +2124,15 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
   }
 }
 
-// r and x of the CTA's cells live in tensor memory (TMEM): all 512 columns,
-// allocated by warp 0; warp w uses TMEM lanes 32 (w % 4) .. + 31 (the
-// quarter it may access), and for its half leaf k columns (w / 4) * 32 + 8 k
-// .. + 7 for r and the same + kResTmemX for x (lane L holds its column's 8
-// cells).  That leaves the registers to 28 warps, and x is read and written
-// in global memory once per solve.
+// r and A p of the CTA's cells live in tensor memory (TMEM): all 512
+// columns, allocated by warp 0; warp w uses TMEM lanes 32 (w % 4) .. + 31
+// (the quarter it may access), and for its half leaf k columns (w / 4) * 32
+// + 8 k .. + 7 for r and the same + kResTmemAp for A p (lane L holds its
+// column's 8 cells).  That leaves the registers to 28 warps, and A p, formed
+// once per iteration for p.Ap, is kept for the update of r.
 constexpr unsigned kResTmemCols = 512;
-constexpr unsigned kResTmemX = 256;
-static_assert((kResWarps + 3) / 4 * kResHL * 8 <= int(kResTmemX), "TMEM columns");
+constexpr unsigned kResTmemAp = 256;
+static_assert((kResWarps + 3) / 4 * kResHL * 8 <= int(kResTmemAp), "TMEM columns");
 __device__ __forceinline__ void tmem_ld8(unsigned t, float (&v)[8]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
                : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
@@ -2141,8 +2156,9 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   float* ps = reinterpret_cast<float*>(res_smem);
   uint8_t* fsm = res_smem + size_t(kResLeaves) * 512 * sizeof(float);
   __shared__ DiagInv<float> tab[16];
-  __shared__ double s_tot[2];
-  __shared__ int s_ok;
+  __shared__ int s_ok, s_done;
+  __shared__ float s_fa, s_fbeta;
+  __shared__ ResScalars q;  // thread 0's
   __shared__ unsigned s_taddr;
   PcgScalars* sc = a.sc;
   const int G = int(gridDim.x);
@@ -2170,7 +2186,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const unsigned tbase = s_taddr + ((32u * unsigned(warp & 3)) << 16) + unsigned(warp >> 2) * 32u;
-  // the warp's half leaves: r and x into TMEM, the face slots
+  // the warp's half leaves: r into TMEM, the face slots
   int nbl[kResHL];
 #pragma unroll
   for (int k = 0; k < kResHL; ++k) {
@@ -2178,31 +2194,33 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     nbl[k] = -1;
     if (hl < 2 * fr.nl) {
       const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
-      const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
       Col<float> r0;
-      ldcol(static_cast<const float*>(a.r), og, r0);
+      ldcol(static_cast<const float*>(a.r), unsigned(h.s) * 512u + unsigned(h.c), r0);
       tmem_st8(tbase + 8u * k, r0.v);
-      ldcol(static_cast<const float*>(a.x), og, r0);
-      tmem_st8(tbase + kResTmemX + 8u * k, r0.v);
       nbl[k] = face_slot_lane(a.nbr, h.s, lane);
     }
   }
   tmem_wait_st();
+  // Thread 0 keeps the scalar state in fp64 and runs the loop test and the
+  // alpha / beta steps (GB300's FP64 pipe is narrow, and the solve's
+  // settings are read once: after the barriers' acquire loads every read of
+  // the scalar block is an L2 round trip); the other threads take the stop
+  // flag and the fp32 alpha and beta from shared memory.
+  int it = sc->iter;
+  if (threadIdx.x == 0) {
+    q = ResScalars{sc->rr, sc->rz, sc->rz_old, 0.0, 0.0, 0.0, sc->status, sc->max_iter, pcg_rule(sc)};
+    s_done = sc->done || it >= q.max_iter || converged(q.rule, q.rr);  // PCGDriver::Solve's loop test
+    s_fbeta = 0.f;
+  }
   __syncthreads();
-  const bool fp32 = sc->fp32 != 0;
-  int it = sc->iter, done = sc->done, status = sc->status;
-  const int max_iter = sc->max_iter;
-  double rz = sc->rz, rr = sc->rr, beta = 0.0, alpha = 0.0, pAp = 0.0, rz_old = sc->rz_old;
   unsigned round = 0;
   bool ok = true;
   float* x = static_cast<float*>(a.x);
   float* rmir = static_cast<float*>(a.r);
-  while (!done) {
-    done = (it >= max_iter) || converged(sc, rr);  // PCGDriver::Solve's loop test
-    if (done) break;
+  while (!s_done) {
     float* pm_new = static_cast<float*>((it & 1) ? a.p1 : a.p0);
     const float* pm_old = static_cast<const float*>((it & 1) ? a.p0 : a.p1);
-    const float fbeta = float(beta);
+    const float fbeta = s_fbeta;
     // S: p = z + beta p on the own columns
 #pragma unroll
     for (int k = 0; k < kResHL; ++k) {
@@ -2234,94 +2252,81 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         Col<float> P, ap;
         ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
-        res_ap<false>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
+        res_ap(fr, a, pm_old, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
 #pragma unroll
         for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
+        tmem_st8(tbase + kResTmemAp + 8u * k, ap.v);
       }
     }
+    tmem_wait_st();
     {
       float v[1] = {dp.pvalue()};
-      double tot[1];
-      if (!(ok = res_sync<1>(a, v, 0, ++round, tot, s_tot, &s_ok))) break;
-      pAp = round_t(sc, tot[0]);
-      alpha = fp32 ? double(__fdiv_rn(float(rz), float(pAp))) : rz / pAp;
-      if (!(alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
-        status = FSIM_ERR_BREAKDOWN;
-        done = 1;
-        break;
-      }
+      ok = res_sync<1>(a, v, 0, ++round, &s_ok, [&](const double (&tot)[1]) {
+        q.pAp = round_t(q.rule, tot[0]);
+        q.alpha = q.rule.fp32 ? double(__fdiv_rn(float(q.rz), float(q.pAp))) : q.rz / q.pAp;
+        s_fa = float(q.alpha);
+        if (!(q.alpha <= 1e5)) {  // CHECK_LE(alpha, LARGE_FLOAT)
+          q.status = FSIM_ERR_BREAKDOWN;
+          s_done = 1;
+        }
+      });
+      if (!ok || s_done) break;
     }
     // U: x += alpha p, r -= alpha A p
-    const float fa = float(alpha), fna = -fa;
+    const float fa = s_fa, fna = -fa;
     Dot<0> drr, drz;
 #pragma unroll
     for (int k = 0; k < kResHL; ++k) {
       const int hl = warp + k * kResWarps;
-      int fs[6];
-      face_slots(nbl[k], fs);
       if (hl < 2 * fr.nl) {
         const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
         const int ol = (hl >> 1) * 512 + h.c;
         const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
-        Col<float> P, ap;
+        Col<float> P, X, R;
+        ldcol(x, og, X);
         ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
-        {
-          float X[8];
-          tmem_ld8(tbase + kResTmemX + 8u * k, X);
 #pragma unroll
-          for (int z = 0; z < 8; ++z) X[z] = tadd(tmul(fa, P.v[z]), X[z]);
-          tmem_st8(tbase + kResTmemX + 8u * k, X);
-        }
-        res_ap<true>(fr, a, pm_old, pm_new, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
-        float rk[8];
-        tmem_ld8(tbase + 8u * k, rk);
+        for (int z = 0; z < 8; ++z) X.v[z] = tadd(tmul(fa, P.v[z]), X.v[z]);
+        stcol(x, og, X);
+        float ap[8];
+        tmem_ld8(tbase + 8u * k, R.v);
+        tmem_ld8(tbase + kResTmemAp + 8u * k, ap);
 #pragma unroll
         for (int z = 0; z < 8; ++z) {
           const uint8_t g = fbyte(f, z);
-          rk[z] = tadd(tmul(fna, ap.v[z]), rk[z]);
-          drr.add(rk[z], rk[z]);
-          drz.add(rk[z], tmul(tab[g & 15].inv, rk[z]));
-          ap.v[z] = rk[z];
+          R.v[z] = tadd(tmul(fna, ap[z]), R.v[z]);
+          drr.add(R.v[z], R.v[z]);
+          drz.add(R.v[z], tmul(tab[g & 15].inv, R.v[z]));
         }
-        tmem_st8(tbase + 8u * k, rk);
-        stcol(rmir, og, ap);
+        tmem_st8(tbase + 8u * k, R.v);
+        stcol(rmir, og, R);
       }
     }
     tmem_wait_st();
     {
       float v[2] = {drr.pvalue(), drz.pvalue()};
-      double tot[2];
-      if (!(ok = res_sync<2>(a, v, 1, ++round, tot, s_tot, &s_ok))) break;
-      rr = round_t(sc, tot[0]);
-      const double rzn = round_t(sc, tot[1]);
-      beta = fp32 ? double(__fdiv_rn(float(rzn), float(rz))) : rzn / rz;
-      rz_old = rz;
-      rz = rzn;
+      ok = res_sync<2>(a, v, 1, ++round, &s_ok, [&](const double (&tot)[2]) {
+        q.rr = round_t(q.rule, tot[0]);
+        const double rzn = round_t(q.rule, tot[1]);
+        q.beta = q.rule.fp32 ? double(__fdiv_rn(float(rzn), float(q.rz))) : rzn / q.rz;
+        q.rz_old = q.rz;
+        q.rz = rzn;
+        s_fbeta = float(q.beta);
+        if (!(q.beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
+          q.status = FSIM_ERR_BREAKDOWN;
+          s_done = 1;
+        } else {
+          s_done = (it + 1 >= q.max_iter) || converged(q.rule, q.rr);  // the next loop test
+        }
+      });
+      if (!ok) break;
       ++it;
-      if (!(beta <= 1e5)) {  // CHECK_LE(beta, LARGE_FLOAT)
-        status = FSIM_ERR_BREAKDOWN;
-        done = 1;
-      }
     }
   }
-  if (!ok) {
-    status = FSIM_ERR_TIMEOUT;
-    done = 1;
-  }
-  // x back to global memory; every warp is then done with TMEM, and warp 0
-  // frees it
+  if (!ok && threadIdx.x == 0) q.status = FSIM_ERR_TIMEOUT;
+  // every warp is done with TMEM; warp 0 frees it
   tmem_wait_st();
-#pragma unroll
-  for (int k = 0; k < kResHL; ++k) {
-    const int hl = warp + k * kResWarps;
-    if (hl < 2 * fr.nl) {
-      const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
-      Col<float> X;
-      tmem_ld8(tbase + kResTmemX + 8u * k, X.v);
-      stcol(x, unsigned(h.s) * 512u + unsigned(h.c), X);
-    }
-  }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   if (warp == 0) {
@@ -2333,13 +2338,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     sc->iter = it;
     sc->done = 1;
-    sc->status = status;
-    sc->rr = rr;
-    sc->rz = rz;
-    sc->rz_old = rz_old;
-    sc->alpha = alpha;
-    sc->beta = beta;
-    sc->pAp = pAp;
+    sc->status = q.status;
+    sc->rr = q.rr;
+    sc->rz = q.rz;
+    sc->rz_old = q.rz_old;
+    sc->alpha = q.alpha;
+    sc->beta = q.beta;
+    sc->pAp = q.pAp;
   }
 }
 
@@ -2794,12 +2799,13 @@ int run_resident(fsim_sim* s, PcgArgs& a, int grid) {
   return FSIM_OK;
 }
 // The resident loop takes fp32 solves whose particle leaves fit (at most
-// kResLeaves per SM) and are many enough to amortise its two grid barriers
-// per iteration (about 4 us each): from kResMinLeaves per SM.  Measured per
-// iteration against the pair: 29.9 against 32.1 us at 256^3 (55 leaves per
-// SM), 12.5 against 12.5 at 128^3, 10.9 against 6.5-7.0 at 64^3 (about one
-// leaf per SM).  FSIM_PCG_RES=0 / 1 turns it off / on wherever it fits.
-constexpr int kResMinLeaves = 16;
+// kResLeaves per SM) and are many enough to amortise its fixed cost per
+// iteration (two grid barriers, about 7.6 us in all): from kResMinLeaves per
+// SM.  Measured per iteration against the pair: 20.95 against 32.1 us at
+// 256^3 (55 leaves per SM), 9.0 against 12.45 at 128^3 (7.6), 7.9 against
+// 6.5-7.0 at 64^3 (about one leaf per SM); the two meet near two leaves per
+// SM.  FSIM_PCG_RES=0 / 1 turns it off / on wherever it fits.
+constexpr int kResMinLeaves = 2;
 bool use_resident(const fsim_sim* s, int precision) {
   if (precision != FSIM_PREC_FP32 || s->pcg_res == 0) return false;
   const int64_t n = s->n_pleaf, sms = s->num_sms;

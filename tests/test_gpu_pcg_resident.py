@@ -6,7 +6,7 @@ thread in another order, so the bars are the solver's own: after a fixed
 number of iterations it tracks the oracle as closely as the pair does, and a
 relative-1e-5 solve is no further from the converged (FP64) solution than the
 oracle's fp32 solve.  By default it takes the fp32 solves of systems with
-16 to 56 particle leaves per SM; FSIM_PCG_RES=1 forces it wherever it fits,
+2 to 56 particle leaves per SM; FSIM_PCG_RES=1 forces it wherever it fits,
 =0 turns it off."""
 import numpy as np
 import pytest
@@ -99,8 +99,9 @@ def test_status_other_precisions_and_default(monkeypatch):
 
 def test_chosen_by_system_size(monkeypatch):
     """Without FSIM_PCG_RES the 256^3 dam break (8,320 particle leaves, 55 per
-    SM) takes the resident loop and a 32^3 system (a few leaves per SM) the
-    pair; with FSIM_PCG_RES=0 the 256^3 system takes the pair."""
+    SM) and the 128^3 sphere drop (1,148, 7.6 per SM) take the resident loop,
+    the 64^3 sphere drop (156, about one per SM) and a 32^3 system the pair;
+    with FSIM_PCG_RES=0 the 256^3 system takes the pair."""
     import torch
 
     monkeypatch.delenv("FSIM_PCG_RES", raising=False)
@@ -109,19 +110,19 @@ def test_chosen_by_system_size(monkeypatch):
     orc, sim = _prepared()
     assert "pcg_resident" not in _loop_kernels(sim, prm)[1]
     sim.close()
-    n = 256
-    g, f = fsim.physical_gravity(n)
-    for env, want in ((None, True), ("0", False)):
+    for n, scene, env, want in ((64, "sphere_drop", None, False), (128, "sphere_drop", None, True),
+                                (256, "dam_break", None, True), (256, "dam_break", "0", False)):
+        g, f = fsim.physical_gravity(n)
         with monkeypatch.context() as m:
             if env is not None:
                 m.setenv("FSIM_PCG_RES", env)
             big = fsim.Simulation((n, n, n), fsim.BOUNDARY_BOX, g, f)
         with big:
-            big.seed(fsim.scene_passes("dam_break", n), seed=0)
+            big.seed(fsim.scene_passes(scene, n), seed=0)
             big.transfer_particles_to_grid()
             big.apply_boundary_conditions()
             big.compute_divergence()
             nl = big.leaves().shape[0]
-            assert 16 * sms <= nl <= 56 * sms, (nl, sms)
+            assert (2 * sms <= nl <= 56 * sms) == (want or env == "0"), (n, nl, sms)
             names = _loop_kernels(big, prm)[1]
-            assert ("pcg_resident" in names) == want, names
+            assert ("pcg_resident" in names) == want, (n, env, names)
