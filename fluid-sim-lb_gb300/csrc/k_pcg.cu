@@ -1931,7 +1931,10 @@ constexpr int kResWarps = 28;
 constexpr int kResThreads = kResWarps * 32;
 constexpr int kResHL = 4;                             // half leaves per warp
 constexpr int kResLeaves = kResWarps * kResHL / 2;    // leaves per CTA
-constexpr size_t kResSmem = size_t(kResLeaves) * 512 * (sizeof(float) + 1);  // p, flags
+// dynamic shared memory: p and the flags of the CTA's leaves, and x of every
+// warp's half leaves 1 .. kResHL - 1 (half leaf 0's x is in tensor memory)
+constexpr size_t kResSmemX = size_t(kResHL - 1) * kResWarps * 256 * sizeof(float);
+constexpr size_t kResSmem = size_t(kResLeaves) * 512 * (sizeof(float) + 1) + kResSmemX;
 constexpr unsigned kResPolls = 1u << 22;  // about 2-4 s of L2 round trips
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
@@ -2129,10 +2132,28 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
 // (the quarter it may access), and for its half leaf k columns (w / 4) * 32
 // + 8 k .. + 7 for r and the same + kResTmemAp for A p (lane L holds its
 // column's 8 cells).  That leaves the registers to 28 warps, and A p, formed
-// once per iteration for p.Ap, is kept for the update of r.
+// once per iteration for p.Ap, is kept for the update of r.  x of half leaf
+// 0 takes columns kResTmemX + (w / 4) * 8 .. + 7; x of half leaves 1 .. 3
+// is in shared memory.  So every vector of the iteration stays on chip, and
+// x is read and written in global memory once per solve.
 constexpr unsigned kResTmemCols = 512;
-constexpr unsigned kResTmemAp = 256;
-static_assert((kResWarps + 3) / 4 * kResHL * 8 <= int(kResTmemAp), "TMEM columns");
+constexpr unsigned kResTmemVec = (kResWarps + 3) / 4 * kResHL * 8;  // columns of r or A p
+constexpr unsigned kResTmemAp = kResTmemVec;
+constexpr unsigned kResTmemX = 2 * kResTmemVec;
+static_assert(kResTmemX + (kResWarps + 3) / 4 * 8 <= kResTmemCols, "TMEM columns");
+
+// x of the warp's half leaf k >= 1 in shared memory: two 16-byte chunks per
+// lane (cells z = 0..3 and 4..7), consecutive lanes in consecutive words
+__device__ __forceinline__ void xs_ld(const float4* xs, int k, int warp, int lane, float (&v)[8]) {
+  const float4 u = xs[(((k - 1) * kResWarps + warp) * 2 + 0) * 32 + lane];
+  const float4 w = xs[(((k - 1) * kResWarps + warp) * 2 + 1) * 32 + lane];
+  v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+  v[4] = w.x; v[5] = w.y; v[6] = w.z; v[7] = w.w;
+}
+__device__ __forceinline__ void xs_st(float4* xs, int k, int warp, int lane, const float (&v)[8]) {
+  xs[(((k - 1) * kResWarps + warp) * 2 + 0) * 32 + lane] = make_float4(v[0], v[1], v[2], v[3]);
+  xs[(((k - 1) * kResWarps + warp) * 2 + 1) * 32 + lane] = make_float4(v[4], v[5], v[6], v[7]);
+}
 __device__ __forceinline__ void tmem_ld8(unsigned t, float (&v)[8]) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
                : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
@@ -2155,6 +2176,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   extern __shared__ __align__(16) unsigned char res_smem[];
   float* ps = reinterpret_cast<float*>(res_smem);
   uint8_t* fsm = res_smem + size_t(kResLeaves) * 512 * sizeof(float);
+  float4* xs = reinterpret_cast<float4*>(res_smem + size_t(kResLeaves) * 512 * (sizeof(float) + 1));
   __shared__ DiagInv<float> tab[16];
   __shared__ int s_ok, s_done;
   __shared__ float s_fa, s_fbeta;
@@ -2186,7 +2208,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const unsigned tbase = s_taddr + ((32u * unsigned(warp & 3)) << 16) + unsigned(warp >> 2) * 32u;
-  // the warp's half leaves: r into TMEM, the face slots
+  const unsigned txb = s_taddr + ((32u * unsigned(warp & 3)) << 16) + kResTmemX + unsigned(warp >> 2) * 8u;
+  // the warp's half leaves: r and x on chip, the face slots
   int nbl[kResHL];
 #pragma unroll
   for (int k = 0; k < kResHL; ++k) {
@@ -2194,9 +2217,15 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     nbl[k] = -1;
     if (hl < 2 * fr.nl) {
       const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+      const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
       Col<float> r0;
-      ldcol(static_cast<const float*>(a.r), unsigned(h.s) * 512u + unsigned(h.c), r0);
+      ldcol(static_cast<const float*>(a.r), og, r0);
       tmem_st8(tbase + 8u * k, r0.v);
+      ldcol(static_cast<const float*>(a.x), og, r0);
+      if (k == 0)
+        tmem_st8(txb, r0.v);
+      else
+        xs_st(xs, k, warp, lane, r0.v);
       nbl[k] = face_slot_lane(a.nbr, h.s, lane);
     }
   }
@@ -2283,12 +2312,18 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         const int ol = (hl >> 1) * 512 + h.c;
         const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
         Col<float> P, X, R;
-        ldcol(x, og, X);
+        if (k == 0)
+          tmem_ld8(txb, X.v);
+        else
+          xs_ld(xs, k, warp, lane, X.v);
         ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
 #pragma unroll
         for (int z = 0; z < 8; ++z) X.v[z] = tadd(tmul(fa, P.v[z]), X.v[z]);
-        stcol(x, og, X);
+        if (k == 0)
+          tmem_st8(txb, X.v);
+        else
+          xs_st(xs, k, warp, lane, X.v);
         float ap[8];
         tmem_ld8(tbase + 8u * k, R.v);
         tmem_ld8(tbase + kResTmemAp + 8u * k, ap);
@@ -2325,8 +2360,22 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     }
   }
   if (!ok && threadIdx.x == 0) q.status = FSIM_ERR_TIMEOUT;
-  // every warp is done with TMEM; warp 0 frees it
+  // x back to global memory; every warp is then done with TMEM, and warp 0
+  // frees it
   tmem_wait_st();
+#pragma unroll
+  for (int k = 0; k < kResHL; ++k) {
+    const int hl = warp + k * kResWarps;
+    if (hl < 2 * fr.nl) {
+      const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+      Col<float> X;
+      if (k == 0)
+        tmem_ld8(txb, X.v);
+      else
+        xs_ld(xs, k, warp, lane, X.v);
+      stcol(x, unsigned(h.s) * 512u + unsigned(h.c), X);
+    }
+  }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   if (warp == 0) {
