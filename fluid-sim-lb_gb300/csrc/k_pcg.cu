@@ -629,19 +629,6 @@ __device__ __forceinline__ void ld_col_sh(const Tile<T>& t, int x, int y, Col<T>
   }
 }
 
-// A z-column (8 cells) of a shared-memory array at float offset c (16-byte
-// aligned): two 16 B shared accesses.
-__device__ __forceinline__ void ld_col_box(const float* box, int c, Col<float>& col) {
-  const float4 u = *reinterpret_cast<const float4*>(box + c);
-  const float4 w = *reinterpret_cast<const float4*>(box + c + 4);
-  col.v[0] = u.x; col.v[1] = u.y; col.v[2] = u.z; col.v[3] = u.w;
-  col.v[4] = w.x; col.v[5] = w.y; col.v[6] = w.z; col.v[7] = w.w;
-}
-__device__ __forceinline__ void st_col_box(float* box, int c, const Col<float>& col) {
-  *reinterpret_cast<float4*>(box + c) = make_float4(col.v[0], col.v[1], col.v[2], col.v[3]);
-  *reinterpret_cast<float4*>(box + c + 4) = make_float4(col.v[4], col.v[5], col.v[6], col.v[7]);
-}
-
 // A p on the lane's column, summed in the reference's column order
 // (-x,-y,-z, diag, +z,+y,+x); 0 off-fluid.  The four x/y neighbour columns
 // come from the tile; zm / zp are the -z / +z face cells.
@@ -1942,13 +1929,6 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-// a column written by another CTA of this launch: through L2, not L1
-__device__ __forceinline__ void ldcol_l2(const float* p, unsigned o, Col<float>& c) {
-  const float4 u = __ldcg(reinterpret_cast<const float4*>(p + o));
-  const float4 w = __ldcg(reinterpret_cast<const float4*>(p + o + 4));
-  c.v[0] = u.x; c.v[1] = u.y; c.v[2] = u.z; c.v[3] = u.w;
-  c.v[4] = w.x; c.v[5] = w.y; c.v[6] = w.z; c.v[7] = w.w;
-}
 
 // Grid barrier of round `round` with the CTA's NV partials: publish, arrive
 // (a GPU-scope release add on one counter, after the CTA barrier that orders
@@ -2058,24 +2038,6 @@ __device__ __forceinline__ bool res_local(const ResFrame& fr, int slot) {
   return slot >= fr.L0 && slot < fr.L0 + fr.nl;
 }
 
-// p (current iteration) of the column at cell offset v of leaf `slot`: from
-// shared memory for the CTA's leaves; else formed from the mirrors of r and
-// the previous p (the owner's operations, so the owner's bits).
-__device__ __forceinline__ void res_pcol(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
-                                         const DiagInv<float>* tab, float beta, int slot, int v,
-                                         Col<float>& out) {
-  if (res_local(fr, slot)) {
-    ps_ldcol(fr.ps, slot - fr.L0, v, out);
-  } else {
-    const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
-    Col<float> r, po;
-    ldcol_l2(static_cast<const float*>(a.r), o, r);
-    ldcol_l2(pm_old, o, po);
-    const uint2 f = ldflags(a.flags, o);
-#pragma unroll
-    for (int z = 0; z < 8; ++z) out.v[z] = pnew_of<float>(tab, fbyte(f, z), r.v[z], po.v[z], beta);
-  }
-}
 __device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
                                            const float* pm_old, const DiagInv<float>* tab,
                                            float beta, int slot, int v) {
@@ -2085,23 +2047,77 @@ __device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
                         __ldcg(pm_old + o), beta);
 }
 
-// A p on the lane's column (x, y) of leaf s (own values P), in the
-// reference's column order; 0 off-fluid.
+// The half leaf's faces in other CTAs' leaves (its outward x face and both
+// y faces: 16 columns of 8 cells), formed by all 32 lanes in step: lane L
+// forms cells 4 (L & 1) .. + 3 of face column t = L >> 1 (t < 8: the x face
+// at y = t; 8 .. 11: the -y face at x = xb + t - 8; 12 .. 15: the +y face)
+// from the mirrors of r and the previous p, with the owner's operations.
+// Faces in the CTA's own leaves are left to shared memory (v stays 0).
+__device__ __forceinline__ void res_faces(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
+                                          const DiagInv<float>* tab, float beta, int xb,
+                                          const int fs[6], int lane, float (&v)[4]) {
+  const int t = lane >> 1;
+  int slot, off;
+  if (t < 8) {
+    slot = xb == 0 ? fs[0] : fs[1];
+    off = (xb == 0 ? 7 : 0) * 64 + t * 8;
+  } else if (t < 12) {
+    slot = fs[2];
+    off = (xb + t - 8) * 64 + 56;
+  } else {
+    slot = fs[3];
+    off = (xb + t - 12) * 64;
+  }
+  off += 4 * (lane & 1);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) v[j] = 0.f;
+  if (!res_local(fr, slot)) {
+    const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(off);
+    const float4 r = __ldcg(reinterpret_cast<const float4*>(static_cast<const float*>(a.r) + o));
+    const float4 po = __ldcg(reinterpret_cast<const float4*>(pm_old + o));
+    const unsigned f = __ldg(reinterpret_cast<const unsigned*>(a.flags + o));
+    v[0] = pnew_of<float>(tab, uint8_t(f), r.x, po.x, beta);
+    v[1] = pnew_of<float>(tab, uint8_t(f >> 8), r.y, po.y, beta);
+    v[2] = pnew_of<float>(tab, uint8_t(f >> 16), r.z, po.z, beta);
+    v[3] = pnew_of<float>(tab, uint8_t(f >> 24), r.w, po.w, beta);
+  }
+}
+// column c of the faces formed by res_faces (lanes 2 c and 2 c + 1)
+__device__ __forceinline__ void res_face_col(const float (&v)[4], int c, Col<float>& out) {
+#pragma unroll
+  for (int z = 0; z < 8; ++z) out.v[z] = __shfl_sync(0xffffffffu, v[z & 3], 2 * c + (z >> 2));
+}
+
+// A p on the lane's column (xb + lx, y) of leaf s (own values P), in the
+// reference's column order; 0 off-fluid.  Called by all 32 lanes of the
+// warp together (res_faces, res_face_col).
 __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
-                                       const DiagInv<float>* tab, float beta, int s, int x, int y,
-                                       const int fs[6], const Col<float>& P, uint2 f,
-                                       Col<float>& ap) {
+                                       const DiagInv<float>* tab, float beta, int s, int xb, int lx,
+                                       int y, int lane, const int fs[6], const Col<float>& P,
+                                       uint2 f, Col<float>& ap) {
+  const int x = xb + lx;
+  float fv[4];
+  res_faces(fr, a, pm_old, tab, beta, xb, fs, lane, fv);
   // one neighbour column at a time, in the reference's order: -x, -y, -z,
   // diag, +z, +y, +x
   Col<float> nc;
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = 0.f;
-  res_pcol(fr, a, pm_old, tab, beta, x > 0 ? s : fs[0],
-              (x > 0 ? x - 1 : 7) * 64 + y * 8, nc);
+  if (xb == 0) res_face_col(fv, y, nc);  // warp-uniform: the outward face is -x
+  if (x > 0)
+    ps_ldcol(fr.ps, s - fr.L0, (x - 1) * 64 + y * 8, nc);
+  else if (res_local(fr, fs[0]))
+    ps_ldcol(fr.ps, fs[0] - fr.L0, 7 * 64 + y * 8, nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
-  res_pcol(fr, a, pm_old, tab, beta, y > 0 ? s : fs[2],
-              x * 64 + (y > 0 ? y - 1 : 7) * 8, nc);
+  Col<float> gy;  // the -y face column for lanes at y = 0, the +y one at y = 7
+  res_face_col(fv, (y == 0 ? 8 : 12) + lx, gy);
+  if (y > 0)
+    ps_ldcol(fr.ps, s - fr.L0, x * 64 + (y - 1) * 8, nc);
+  else if (res_local(fr, fs[2]))
+    ps_ldcol(fr.ps, fs[2] - fr.L0, x * 64 + 7 * 8, nc);
+  else
+    nc = gy;
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
   const float zm = res_pcell(fr, a, pm_old, tab, beta, fs[4], x * 64 + y * 8 + 7);
@@ -2114,12 +2130,19 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
     ap.v[z] = tadd(ap.v[z], tmul(tab[g & 15].d, P.v[z]));
     ap.v[z] = tsub(ap.v[z], vzp);
   }
-  res_pcol(fr, a, pm_old, tab, beta, y < 7 ? s : fs[3],
-              x * 64 + (y < 7 ? y + 1 : 0) * 8, nc);
+  if (y < 7)
+    ps_ldcol(fr.ps, s - fr.L0, x * 64 + (y + 1) * 8, nc);
+  else if (res_local(fr, fs[3]))
+    ps_ldcol(fr.ps, fs[3] - fr.L0, x * 64, nc);
+  else
+    nc = gy;
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
-  res_pcol(fr, a, pm_old, tab, beta, x < 7 ? s : fs[1],
-              (x < 7 ? x + 1 : 0) * 64 + y * 8, nc);
+  if (xb != 0) res_face_col(fv, y, nc);  // the outward face is +x
+  if (x < 7)
+    ps_ldcol(fr.ps, s - fr.L0, (x + 1) * 64 + y * 8, nc);
+  else if (res_local(fr, fs[1]))
+    ps_ldcol(fr.ps, fs[1] - fr.L0, y * 8, nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) {
     ap.v[z] = tsub(ap.v[z], nc.v[z]);
@@ -2281,7 +2304,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         Col<float> P, ap;
         ps_ldcol(ps, hl >> 1, h.c, P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
-        res_ap(fr, a, pm_old, tab, fbeta, h.s, h.xb + h.lx, h.cy, fs, P, f, ap);
+        res_ap(fr, a, pm_old, tab, fbeta, h.s, h.xb, h.lx, h.cy, lane, fs, P, f, ap);
 #pragma unroll
         for (int z = 0; z < 8; ++z) dp.add(P.v[z], ap.v[z]);
         tmem_st8(tbase + kResTmemAp + 8u * k, ap.v);
