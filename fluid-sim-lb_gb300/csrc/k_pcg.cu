@@ -1945,57 +1945,60 @@ template <int NV, typename F>
 __device__ __forceinline__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0,
                                          unsigned round, int* s_ok, F&& fin) {
   block_sum_p<float, NV, kResThreads>(v);  // its CTA barrier orders the CTA's stores first
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) a.partf[(row0 + k) * a.maxb + blockIdx.x] = v[k];
-    asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(&a.sc->bar_count) : "memory");
-    const unsigned target = round * gridDim.x;
-    unsigned polls = 0;
-    int ok = 1;
-    while (ld_acquire_gpu(&a.sc->bar_count) < target) {
-      if ((++polls & 255u) == 0u &&
-          (polls > kResPolls || ld_acquire_gpu(&a.sc->bar_err) != 0u)) {
-        ok = 0;
-        break;
-      }
-    }
-    if (!ok) atomicExch(&a.sc->bar_err, 1u);
-    *s_ok = ok;
-  }
-  __syncthreads();
-  if (!*s_ok) return false;
   if (threadIdx.x < 32) {
-    // lane adds partials lane, lane + 32, ... in that order; each batch's
-    // loads are all issued before its adds (a zero pad adds exactly nothing)
+    // warp 0: lane 0 publishes, arrives and waits; the warp then sums
     const int lane = threadIdx.x, G = int(gridDim.x);
-    float x[NV];
+    int ok = 1;
+    if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < NV; ++k) x[k] = 0.f;
-    for (int i0 = lane; i0 < G; i0 += 32 * 8) {
-      float t[NV][8];
-#pragma unroll
-      for (int k = 0; k < NV; ++k)
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int i = i0 + 32 * u;
-          t[k][u] = i < G ? __ldcg(a.partf + (row0 + k) * a.maxb + i) : 0.f;
+      for (int k = 0; k < NV; ++k) a.partf[(row0 + k) * a.maxb + blockIdx.x] = v[k];
+      asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(&a.sc->bar_count) : "memory");
+      const unsigned target = round * gridDim.x;
+      unsigned polls = 0;
+      while (ld_acquire_gpu(&a.sc->bar_count) < target) {
+        if ((++polls & 255u) == 0u &&
+            (polls > kResPolls || ld_acquire_gpu(&a.sc->bar_err) != 0u)) {
+          ok = 0;
+          break;
         }
-#pragma unroll
-      for (int k = 0; k < NV; ++k)
-#pragma unroll
-        for (int u = 0; u < 8; ++u) x[k] = __fadd_rn(x[k], t[k][u]);
+      }
+      if (!ok) atomicExch(&a.sc->bar_err, 1u);
+      *s_ok = ok;
     }
-    double tot[NV];
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();  // orders lane 0's acquire before the other lanes' loads
+    if (ok) {
+      // lane adds partials lane, lane + 32, ... in that order; each batch's
+      // loads are all issued before its adds (a zero pad adds exactly nothing)
+      float x[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
+      for (int k = 0; k < NV; ++k) x[k] = 0.f;
+      for (int i0 = lane; i0 < G; i0 += 32 * 8) {
+        float t[NV][8];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) x[k] = __fadd_rn(x[k], __shfl_down_sync(0xffffffffu, x[k], o));
-      tot[k] = double(x[k]);
+        for (int k = 0; k < NV; ++k)
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int i = i0 + 32 * u;
+            t[k][u] = i < G ? __ldcg(a.partf + (row0 + k) * a.maxb + i) : 0.f;
+          }
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+#pragma unroll
+          for (int u = 0; u < 8; ++u) x[k] = __fadd_rn(x[k], t[k][u]);
+      }
+      double tot[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x[k] = __fadd_rn(x[k], __shfl_down_sync(0xffffffffu, x[k], o));
+        tot[k] = double(x[k]);
+      }
+      if (lane == 0) fin(tot);
     }
-    if (lane == 0) fin(tot);
   }
   __syncthreads();
-  return true;
+  return *s_ok != 0;
 }
 
 // Shared p of the CTA's leaves in 16-byte chunk planes: float4 element
@@ -2232,8 +2235,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const unsigned tbase = s_taddr + ((32u * unsigned(warp & 3)) << 16) + unsigned(warp >> 2) * 32u;
   const unsigned txb = s_taddr + ((32u * unsigned(warp & 3)) << 16) + kResTmemX + unsigned(warp >> 2) * 8u;
-  // the warp's half leaves: r and x on chip, the face slots
+  // the warp's half leaves: r and x on chip, the face slots, and which of
+  // the lane's columns other CTAs read (bit k of mir: the column is on a face
+  // whose neighbour leaf is in another CTA, or the leaf's -z or +z neighbour
+  // is, which reads a cell of every column); only those go to the mirrors
   int nbl[kResHL];
+  unsigned mir = 0;
 #pragma unroll
   for (int k = 0; k < kResHL; ++k) {
     const int hl = warp + k * kResWarps;
@@ -2250,6 +2257,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
       else
         xs_st(xs, k, warp, lane, r0.v);
       nbl[k] = face_slot_lane(a.nbr, h.s, lane);
+      int fs[6];
+      face_slots(nbl[k], fs);
+      const bool xo = h.xb == 0 ? (h.lx == 0 && !res_local(fr, fs[0]))
+                                : (h.lx == 3 && !res_local(fr, fs[1]));
+      const bool yo = (h.cy == 0 && !res_local(fr, fs[2])) || (h.cy == 7 && !res_local(fr, fs[3]));
+      const bool zo = !res_local(fr, fs[4]) || !res_local(fr, fs[5]);
+      if (xo || yo || zo) mir |= 1u << k;
     }
   }
   tmem_wait_st();
@@ -2288,7 +2302,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
 #pragma unroll
         for (int z = 0; z < 8; ++z) P.v[z] = pnew_of<float>(tab, fbyte(f, z), rk[z], P.v[z], fbeta);
         ps_stcol(ps, hl >> 1, h.c, P);
-        stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
+        if ((mir >> k) & 1u) stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
       }
     }
     __syncthreads();
@@ -2358,7 +2372,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
           drz.add(R.v[z], tmul(tab[g & 15].inv, R.v[z]));
         }
         tmem_st8(tbase + 8u * k, R.v);
-        stcol(rmir, og, R);
+        if ((mir >> k) & 1u) stcol(rmir, og, R);
       }
     }
     tmem_wait_st();
@@ -2383,20 +2397,23 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
     }
   }
   if (!ok && threadIdx.x == 0) q.status = FSIM_ERR_TIMEOUT;
-  // x back to global memory; every warp is then done with TMEM, and warp 0
-  // frees it
+  // x and r back to global memory; every warp is then done with TMEM, and
+  // warp 0 frees it
   tmem_wait_st();
 #pragma unroll
   for (int k = 0; k < kResHL; ++k) {
     const int hl = warp + k * kResWarps;
     if (hl < 2 * fr.nl) {
       const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
+      const unsigned og = unsigned(h.s) * 512u + unsigned(h.c);
       Col<float> X;
       if (k == 0)
         tmem_ld8(txb, X.v);
       else
         xs_ld(xs, k, warp, lane, X.v);
-      stcol(x, unsigned(h.s) * 512u + unsigned(h.c), X);
+      stcol(x, og, X);
+      tmem_ld8(tbase + 8u * k, X.v);
+      stcol(rmir, og, X);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
