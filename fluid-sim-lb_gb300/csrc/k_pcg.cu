@@ -1892,28 +1892,33 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1_s(const __grid_const
 }
 
 // ---- on-chip resident loop: one persistent CTA per SM ---------------------------
-// fp32 solves whose particle leaves fit on chip (FSIM_PCG_RES=1): one
+// fp32 solves whose particle leaves fit on chip (by default 2 to kResLeaves
+// particle leaves per SM; FSIM_PCG_RES=1 / 0 forces it on / off): one
 // cooperative launch runs every iteration.  CTA c owns the contiguous slots
 // [c * per, c * per + nl), per = ceil(n_pleaf / G) <= kResLeaves, and keeps
-// them resident: r in registers (each warp owns up to kResHL half leaves, a
-// lane one z-column of each), p and the flags in shared memory.  Per
-// iteration, as the reference's ComputeLocal1-3 (common/solver.cc:297-366):
-//   S: p = z + beta p on the own columns (into shared memory and a global
-//      mirror), then A p and the p.Ap partials;
+// every vector of the iteration on chip: p and the flags in shared memory,
+// r and A p in tensor memory, x in tensor and shared memory (each warp owns
+// up to kResHL half leaves, a lane one z-column of each).  Per iteration,
+// as the reference's ComputeLocal1-3 (common/solver.cc:297-366):
+//   S: p = z + beta p on the own columns (into shared memory, and the
+//      columns other CTAs read into a global mirror), then A p (kept) and
+//      the p.Ap partials;
 //   grid barrier: every CTA sums the G partials in CTA order -> alpha;
-//   U: A p again, x += alpha p (global), r -= alpha A p (registers, and a
+//   U: x += alpha p, r -= alpha A p (the columns other CTAs read also into a
 //      global mirror), the r.r and r.z partials;
 //   grid barrier -> r.r, r.z, beta and the loop test.
 // Stencil neighbours in the CTA's own leaves come from shared memory; those
-// in other CTAs' leaves from the mirrors, read through L2 (written in this
-// launch): in S the neighbour's p is formed from its r and previous p (the
-// owner's operations, so the owner's bits; p alternates between two mirror
-// buffers by iteration parity), in U it is read from the p mirror.  A p is
-// summed in the reference's column order.  The dot products are summed per
-// thread, per CTA and over CTAs in fixed orders: the solve is deterministic
-// (its per-thread order differs from the pair's, so the bits do too).
-// Barrier waits are bounded (kResPolls); a CTA that gives up sets bar_err and
-// every CTA leaves the loop (FSIM_ERR_TIMEOUT).
+// in other CTAs' leaves are formed from the mirrors of r and the previous p,
+// read through L2 (the owner's operations, so the owner's bits; p alternates
+// between two mirror buffers by iteration parity), by all 32 lanes of the
+// warp together and handed out by warp shuffles.  A p is summed in the
+// reference's column order.  The dot products are summed per thread, per
+// CTA and over CTAs in fixed orders: the solve is deterministic (its
+// per-thread order differs from the pair's, so the bits do too).  Thread 0
+// alone runs the scalar steps (alpha, beta, the loop test) in fp64.  x and r
+// are written back whole at the end.  Barrier waits are bounded (kResPolls);
+// a CTA that gives up sets bar_err and every CTA leaves the loop
+// (FSIM_ERR_TIMEOUT), freeing its tensor memory.
 constexpr int kResWarps = 28;
 constexpr int kResThreads = kResWarps * 32;
 constexpr int kResHL = 4;                             // half leaves per warp
@@ -1940,7 +1945,10 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 // next barrier, and so has read them.  Waits are bounded: a CTA that gives
 // up sets bar_err, which the others also poll.  (Publishing each partial
 // beside the round number in one 64-bit word, polled by every CTA, measured
-// slower: 33.2 against 30.1 us per iteration at 256^3.)
+// slower: 33.2 against 30.1 us per iteration at 256^3, and again with
+// relaxed words and no fence on the p.Ap barrier, 21.8 against 16.8: the
+// polling of 152 slots by every CTA costs more than the counter's second
+// round trip.)
 template <int NV, typename F>
 __device__ __forceinline__ bool res_sync(const PcgArgs& a, float (&v)[NV], int row0,
                                          unsigned round, int* s_ok, F&& fin) {
