@@ -258,6 +258,7 @@ int fsim_create(const fsim_config* cfg, fsim_t** out) {
   // FSIM_PCG_TMA_WITHHOLD=1 (tests): the first solve's bulk-copy spmv holds one
   // stage's flags copy back until its wait has given up
   if (const char* c = std::getenv("FSIM_PCG_TMA_WITHHOLD")) s->tma_withhold = c[0] == '1';
+  if (const char* c = std::getenv("FSIM_PCG_RES_WITHHOLD")) s->res_withhold = c[0] == '1';
   // FSIM_PCG_PIPE=0: the unpipelined hot kernels
   if (const char* c = std::getenv("FSIM_PCG_PIPE")) s->use_pipe = c[0] != '0';
   // FSIM_PCG_CG1=1: fp32 solves by the single-reduction iteration (opt-in)

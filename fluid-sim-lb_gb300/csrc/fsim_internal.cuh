@@ -306,6 +306,10 @@ struct fsim_sim {
   // bounded wait has given up (FSIM_PCG_TMA_WITHHOLD=1)
   int tma_spmv = 0;
   int tma_withhold = 0;
+  // FSIM_PCG_RES_WITHHOLD=1 (tests): in the first solve CTA 0 of the resident
+  // loop skips its first barrier arrival, so that every CTA's bounded wait
+  // gives up
+  int res_withhold = 0;
   // register-pipelined hot kernels (next half leaf loaded during the
   // current; fp32 vectors only: 2% faster per iteration at 256^3)
   bool use_pipe = true;

@@ -304,6 +304,7 @@ struct PcgArgs {
   int init_r;       // setup: 1 -> r = b (x0 = 0); 0 -> r already holds the rhs
   int par;          // spmv / update: parity of the iteration this launch serves
   int withhold;     // bulk-copy spmv, test only: CTA 0's first stage withholds its flags copy
+  int res_withhold; // resident loop, test only: CTA 0 skips its first barrier arrival
   cudaGraphConditionalHandle cond;  // WHILE-node handle when run as a graph, else 0
   void* w[2];       // single-reduction CG: w = A M r (by parity), or null
   void* sv[2];      // single-reduction CG: s = A p (by parity)
@@ -1943,7 +1944,9 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 // barrier.  Rows row0.. of the float partials; each phase type has
 // its own rows, which a CTA can only rewrite after every CTA has passed the
 // next barrier, and so has read them.  Waits are bounded: a CTA that gives
-// up sets bar_err, which the others also poll.  (Publishing each partial
+// up sets bar_err, which the others also poll.  With PcgArgs::res_withhold
+// (tests) CTA 0 does not arrive at the first barrier and the limit is 256
+// polls, so every CTA's wait gives up.  (Publishing each partial
 // beside the round number in one 64-bit word, polled by every CTA, measured
 // slower: 33.2 against 30.1 us per iteration at 256^3, and again with
 // relaxed words and no fence on the p.Ap barrier, 21.8 against 16.8: the
@@ -1960,12 +1963,14 @@ __device__ __forceinline__ bool res_sync(const PcgArgs& a, float (&v)[NV], int r
     if (lane == 0) {
 #pragma unroll
       for (int k = 0; k < NV; ++k) a.partf[(row0 + k) * a.maxb + blockIdx.x] = v[k];
-      asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(&a.sc->bar_count) : "memory");
+      if (!(a.res_withhold && blockIdx.x == 0 && round == 1))
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;\n" ::"l"(&a.sc->bar_count) : "memory");
       const unsigned target = round * gridDim.x;
+      const unsigned limit = a.res_withhold ? 256u : kResPolls;
       unsigned polls = 0;
       while (ld_acquire_gpu(&a.sc->bar_count) < target) {
         if ((++polls & 255u) == 0u &&
-            (polls > kResPolls || ld_acquire_gpu(&a.sc->bar_err) != 0u)) {
+            (polls > limit || ld_acquire_gpu(&a.sc->bar_err) != 0u)) {
           ok = 0;
           break;
         }
@@ -2978,6 +2983,8 @@ int pcg_solve(fsim_sim* s, const fsim_pcg_params* prm, fsim_pcg_stats* st, const
   a.init_r = 1;
   a.withhold = s->tma_withhold;
   s->tma_withhold = 0;  // a test's withheld copy applies to one solve
+  a.res_withhold = s->res_withhold;
+  s->res_withhold = 0;  // and a withheld barrier arrival too
 
   PcgScalars h;
   memset(&h, 0, sizeof(h));

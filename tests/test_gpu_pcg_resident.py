@@ -126,3 +126,28 @@ def test_chosen_by_system_size(monkeypatch):
             assert (2 * sms <= nl <= 56 * sms) == (want or env == "0"), (n, nl, sms)
             names = _loop_kernels(big, prm)[1]
             assert ("pcg_resident" in names) == want, (n, env, names)
+
+
+def test_barrier_wait_gives_up_and_recovers(monkeypatch):
+    """The grid-barrier waits are bounded.  With FSIM_PCG_RES_WITHHOLD=1 CTA 0
+    of the first solve does not arrive at its first barrier (and the limit is
+    256 polls), so every CTA's wait gives up without a fault: each leaves the
+    loop, frees its tensor memory, and the solve reports FSIM_ERR_TIMEOUT.
+    The handle's next solve runs normally, bit for bit as a handle that never
+    timed out."""
+    prm = fsim.pcg_params(fsim.PCG_RELATIVE, fsim.PREC_FP32, 3000, tolerance=1e-5)
+    orc, ref = _prepared_res(monkeypatch)
+    st_ref = ref.pcg_solve(prm)
+    x_ref = ref.field(fsim.FIELD_PRESSURE)[0]
+    ref.close()
+    with monkeypatch.context() as m:
+        m.setenv("FSIM_PCG_RES", "1")
+        m.setenv("FSIM_PCG_RES_WITHHOLD", "1")
+        orc, sim = _prepared()
+    with pytest.raises(fsim.FsimError) as err:
+        sim.pcg_solve(prm)
+    assert err.value.code == fsim.ERR_TIMEOUT
+    st = sim.pcg_solve(prm)  # the withheld arrival applied to one solve only
+    assert st.status == 0 and (st.iterations, st.rr) == (st_ref.iterations, st_ref.rr)
+    assert np.array_equal(sim.field(fsim.FIELD_PRESSURE)[0], x_ref)
+    sim.close()
