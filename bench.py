@@ -76,13 +76,19 @@ UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50, "pcg_cg1": 50, "pcg_resid
 # the timed loop, where the vectors stay in L2 and DRAM mostly sees write-backs.  Scaled by
 # each step's unknowns.  The MIXED pair: a capture at 1024^3 (111,452,816 unknowns, caches
 # flushed; the vectors do not fit in L2 there), the size its solver is benchmarked at.
+# The resident loop: one launch is a whole solve, so its DRAM bytes (48.27 MB read + 23.45 MB
+# written) are divided by the solve's 779 iterations: a capture of the timed step of the
+# 256^3 dam break (about 4.03 M unknowns) with the default bench settings.
 NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": (1.4706e6 + 17.5451e6) / 4021250,
                            "pcg_update": (5.4866e6 + 19.9465e6) / 4021250,
                            "pcg_spmv_mixed": 1.5765e9 / 111452816,
-                           "pcg_update_mixed": 2.3834e9 / 111452816}
-NCU_TRAFFIC_SOURCE = {"pcg_spmv": "256^3, caches not flushed", "pcg_update": "256^3, caches not flushed",
-                      "pcg_spmv_mixed": "1024^3, caches flushed",
-                      "pcg_update_mixed": "1024^3, caches flushed"}
+                           "pcg_update_mixed": 2.3834e9 / 111452816,
+                           "pcg_resident": (48.265984e6 + 23.447552e6) / 779 / 4.03e6}
+NCU_TRAFFIC_SOURCE = {"pcg_spmv": "the 256^3 system, caches not flushed",
+                      "pcg_update": "the 256^3 system, caches not flushed",
+                      "pcg_spmv_mixed": "the 1024^3 system, caches flushed",
+                      "pcg_update_mixed": "the 1024^3 system, caches flushed",
+                      "pcg_resident": "the 256^3 system, one solve's launch over its 779 iterations"}
 # The two launches of one PCG iteration (spmv then update) are reported as one unit: the
 # split of the iteration's work between them is a design choice (the update could take
 # x += alpha p or leave it), and their times are nearly equal.
@@ -434,8 +440,13 @@ def roofline(res):
             out["unfused_frac"] = achieved * ub / per / peak
         if all(k in NCU_TRAFFIC_PER_UNKNOWN for k in names):
             out["traffic"] = sum(NCU_TRAFFIC_PER_UNKNOWN[k] for k in names) * n_rows
-            out["traffic_source"] = (f"ncu capture of the {NCU_TRAFFIC_SOURCE[names[0]]} system "
-                                     "(spmv + update), scaled by unknowns")
+            out["traffic_source"] = (f"ncu capture ({NCU_TRAFFIC_SOURCE[names[0]]}) of "
+                                     f"{' + '.join(names)}, per iteration, scaled by unknowns")
+        if name == "pcg_resident":
+            out["note"] = ("the resident loop keeps every vector of the iteration on chip (shared and "
+                           "tensor memory); achieved counts the streamed formulation's 34 B per unknown, "
+                           "so frac above 1 means the loop beats the HBM roofline of a streaming "
+                           "iteration; its own DRAM traffic is `traffic`")
         pit = sum(res["piters"])
         prow = sum(r * it for r, it in zip(res["prows"], res["piters"]))
         out["per_kernel_profiled"] = {
@@ -447,7 +458,7 @@ def roofline(res):
                share_of_step=tot_ms / res["prof_ms"] if res["prof_ms"] > 0 else None)
     if name in NCU_TRAFFIC_PER_UNKNOWN and res["prows"]:
         out["traffic"] = NCU_TRAFFIC_PER_UNKNOWN[name] * float(np.mean(res["prows"]))
-        out["traffic_source"] = f"ncu capture of the {NCU_TRAFFIC_SOURCE[name]} system, scaled by unknowns"
+        out["traffic_source"] = f"ncu capture ({NCU_TRAFFIC_SOURCE[name]}), scaled by unknowns"
     if name in ALG_BYTES and res["prows"]:
         alg = ALG_BYTES[name] * float(np.mean(res["prows"]))
         tot_bytes = sum(ALG_BYTES[name] * r * it for r, it in zip(res["prows"], res["piters"]))
