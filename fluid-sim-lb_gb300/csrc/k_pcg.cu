@@ -2171,7 +2171,8 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
 // (the quarter it may access), and for its half leaf k columns (w / 4) * 32
 // + 8 k .. + 7 for r and the same + kResTmemAp for A p (lane L holds its
 // column's 8 cells).  That leaves the registers to 28 warps, and A p, formed
-// once per iteration for p.Ap, is kept for the update of r.  x of half leaf
+// once per iteration for p.Ap, is kept for the update of r; from then to the
+// next S its columns hold z = M r, formed once for r.z and p = z + beta p.  x of half leaf
 // 0 takes columns kResTmemX + (w / 4) * 8 .. + 7; x of half leaves 1 .. 3
 // is in shared memory.  So every vector of the iteration stays on chip, and
 // x is read and written in global memory once per solve.
@@ -2264,6 +2265,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
       Col<float> r0;
       ldcol(static_cast<const float*>(a.r), og, r0);
       tmem_st8(tbase + 8u * k, r0.v);
+      {
+        const uint2 f = *reinterpret_cast<const uint2*>(fsm + (hl >> 1) * 512 + h.c);
+        float z0[8];
+#pragma unroll
+        for (int z = 0; z < 8; ++z) z0[z] = tmul(tab[fbyte(f, z) & 15].inv, r0.v[z]);
+        tmem_st8(tbase + kResTmemAp + 8u * k, z0);
+      }
       ldcol(static_cast<const float*>(a.x), og, r0);
       if (k == 0)
         tmem_st8(txb, r0.v);
@@ -2306,14 +2314,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
       const int hl = warp + k * kResWarps;
       if (hl < 2 * fr.nl) {
         const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
-        const int ol = (hl >> 1) * 512 + h.c;
         Col<float> P;
         ps_ldcol(ps, hl >> 1, h.c, P);
-        const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
-        float rk[8];
-        tmem_ld8(tbase + 8u * k, rk);
+        float zk[8];  // z = M r, left in the A p columns by U (or the set-up)
+        tmem_ld8(tbase + kResTmemAp + 8u * k, zk);
 #pragma unroll
-        for (int z = 0; z < 8; ++z) P.v[z] = pnew_of<float>(tab, fbyte(f, z), rk[z], P.v[z], fbeta);
+        for (int z = 0; z < 8; ++z) P.v[z] = tadd(zk[z], tmul(fbeta, P.v[z]));  // pnew_of's operations
         ps_stcol(ps, hl >> 1, h.c, P);
         if ((mir >> k) & 1u) stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
       }
@@ -2382,9 +2388,11 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
           const uint8_t g = fbyte(f, z);
           R.v[z] = tadd(tmul(fna, ap[z]), R.v[z]);
           drr.add(R.v[z], R.v[z]);
-          drz.add(R.v[z], tmul(tab[g & 15].inv, R.v[z]));
+          ap[z] = tmul(tab[g & 15].inv, R.v[z]);  // z = M r, for r.z and the next S
+          drz.add(R.v[z], ap[z]);
         }
         tmem_st8(tbase + 8u * k, R.v);
+        tmem_st8(tbase + kResTmemAp + 8u * k, ap);
         if ((mir >> k) & 1u) stcol(rmir, og, R);
       }
     }
