@@ -2017,24 +2017,20 @@ __device__ __forceinline__ bool res_sync(const PcgArgs& a, float (&v)[NV], int r
 // Shared p of the CTA's leaves in 16-byte chunk planes: float4 element
 // ((leaf * 2 + chunk) * 8 + x) * 8 + y holds the cells z = 4 chunk ..
 // 4 chunk + 3 of column (x, y), so the lanes of a quarter warp (consecutive
-// y) touch consecutive 16-byte words.  v is a cell offset x*64 + y*8 + z.
-__device__ __forceinline__ int ps_chunk(int leaf, int v, int chunk) {
-  return ((leaf * 2 + chunk) * 8 + (v >> 6)) * 8 + ((v >> 3) & 7);
-}
-__device__ __forceinline__ void ps_ldcol(const float* ps, int leaf, int v, Col<float>& c) {
+// y) touch consecutive 16-byte words.  ps_col4 is the float4 index of chunk 0
+// of a column; chunk 1 is 64 further, and the in-leaf neighbour columns are
+// -8 / +8 (x) and -1 / +1 (y) away, constant offsets from the own column.
+__device__ __forceinline__ int ps_col4(int leaf, int x, int y) { return (leaf * 16 + x) * 8 + y; }
+__device__ __forceinline__ void ps_ld4(const float* ps, int i, Col<float>& c) {
   const float4* q = reinterpret_cast<const float4*>(ps);
-  const float4 u = q[ps_chunk(leaf, v, 0)], w = q[ps_chunk(leaf, v, 1)];
+  const float4 u = q[i], w = q[i + 64];
   c.v[0] = u.x; c.v[1] = u.y; c.v[2] = u.z; c.v[3] = u.w;
   c.v[4] = w.x; c.v[5] = w.y; c.v[6] = w.z; c.v[7] = w.w;
 }
-__device__ __forceinline__ void ps_stcol(float* ps, int leaf, int v, const Col<float>& c) {
+__device__ __forceinline__ void ps_st4(float* ps, int i, const Col<float>& c) {
   float4* q = reinterpret_cast<float4*>(ps);
-  q[ps_chunk(leaf, v, 0)] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
-  q[ps_chunk(leaf, v, 1)] = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
-}
-__device__ __forceinline__ float ps_cell(const float* ps, int leaf, int v) {
-  const int z = v & 7;
-  return ps[ps_chunk(leaf, v, z >> 2) * 4 + (z & 3)];
+  q[i] = make_float4(c.v[0], c.v[1], c.v[2], c.v[3]);
+  q[i + 64] = make_float4(c.v[4], c.v[5], c.v[6], c.v[7]);
 }
 
 // The resident loop's scalar state, kept by thread 0.
@@ -2054,11 +2050,13 @@ __device__ __forceinline__ bool res_local(const ResFrame& fr, int slot) {
   return slot >= fr.L0 && slot < fr.L0 + fr.nl;
 }
 
+// p (current iteration) of cell (x, y, z) of leaf `slot`: from shared memory
+// for the CTA's leaves, else formed from the mirrors of r and the previous p.
 __device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
                                            const float* pm_old, const DiagInv<float>* tab,
-                                           float beta, int slot, int v) {
-  if (res_local(fr, slot)) return ps_cell(fr.ps, slot - fr.L0, v);
-  const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(v);
+                                           float beta, int slot, int x, int y, int z) {
+  if (res_local(fr, slot)) return fr.ps[(ps_col4(slot - fr.L0, x, y) + (z >> 2) * 64) * 4 + (z & 3)];
+  const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(x * 64 + y * 8 + z);
   return pnew_of<float>(tab, a.flags[o], __ldcg(static_cast<const float*>(a.r) + o),
                         __ldcg(pm_old + o), beta);
 }
@@ -2112,6 +2110,7 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
                                        int y, int lane, const int fs[6], const Col<float>& P,
                                        uint2 f, Col<float>& ap) {
   const int x = xb + lx;
+  const int own = ps_col4(s - fr.L0, x, y);
   float fv[4];
   res_faces(fr, a, pm_old, tab, beta, xb, fs, lane, fv);
   // one neighbour column at a time, in the reference's order: -x, -y, -z,
@@ -2121,23 +2120,23 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
   for (int z = 0; z < 8; ++z) ap.v[z] = 0.f;
   if (xb == 0) res_face_col(fv, y, nc);  // warp-uniform: the outward face is -x
   if (x > 0)
-    ps_ldcol(fr.ps, s - fr.L0, (x - 1) * 64 + y * 8, nc);
+    ps_ld4(fr.ps, own - 8, nc);
   else if (res_local(fr, fs[0]))
-    ps_ldcol(fr.ps, fs[0] - fr.L0, 7 * 64 + y * 8, nc);
+    ps_ld4(fr.ps, ps_col4(fs[0] - fr.L0, 7, y), nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
   Col<float> gy;  // the -y face column for lanes at y = 0, the +y one at y = 7
   res_face_col(fv, (y == 0 ? 8 : 12) + lx, gy);
   if (y > 0)
-    ps_ldcol(fr.ps, s - fr.L0, x * 64 + (y - 1) * 8, nc);
+    ps_ld4(fr.ps, own - 1, nc);
   else if (res_local(fr, fs[2]))
-    ps_ldcol(fr.ps, fs[2] - fr.L0, x * 64 + 7 * 8, nc);
+    ps_ld4(fr.ps, ps_col4(fs[2] - fr.L0, x, 7), nc);
   else
     nc = gy;
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
-  const float zm = res_pcell(fr, a, pm_old, tab, beta, fs[4], x * 64 + y * 8 + 7);
-  const float zp = res_pcell(fr, a, pm_old, tab, beta, fs[5], x * 64 + y * 8);
+  const float zm = res_pcell(fr, a, pm_old, tab, beta, fs[4], x, y, 7);
+  const float zp = res_pcell(fr, a, pm_old, tab, beta, fs[5], x, y, 0);
 #pragma unroll
   for (int z = 0; z < 8; ++z) {
     const uint8_t g = fbyte(f, z);
@@ -2147,18 +2146,18 @@ __device__ __forceinline__ void res_ap(const ResFrame& fr, const PcgArgs& a, con
     ap.v[z] = tsub(ap.v[z], vzp);
   }
   if (y < 7)
-    ps_ldcol(fr.ps, s - fr.L0, x * 64 + (y + 1) * 8, nc);
+    ps_ld4(fr.ps, own + 1, nc);
   else if (res_local(fr, fs[3]))
-    ps_ldcol(fr.ps, fs[3] - fr.L0, x * 64, nc);
+    ps_ld4(fr.ps, ps_col4(fs[3] - fr.L0, x, 0), nc);
   else
     nc = gy;
 #pragma unroll
   for (int z = 0; z < 8; ++z) ap.v[z] = tsub(ap.v[z], nc.v[z]);
   if (xb != 0) res_face_col(fv, y, nc);  // the outward face is +x
   if (x < 7)
-    ps_ldcol(fr.ps, s - fr.L0, (x + 1) * 64 + y * 8, nc);
+    ps_ld4(fr.ps, own + 8, nc);
   else if (res_local(fr, fs[1]))
-    ps_ldcol(fr.ps, fs[1] - fr.L0, y * 8, nc);
+    ps_ld4(fr.ps, ps_col4(fs[1] - fr.L0, 0, y), nc);
 #pragma unroll
   for (int z = 0; z < 8; ++z) {
     ap.v[z] = tsub(ap.v[z], nc.v[z]);
@@ -2315,12 +2314,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
       if (hl < 2 * fr.nl) {
         const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
         Col<float> P;
-        ps_ldcol(ps, hl >> 1, h.c, P);
+        const int own = ps_col4(hl >> 1, h.xb + h.lx, h.cy);
+        ps_ld4(ps, own, P);
         float zk[8];  // z = M r, left in the A p columns by U (or the set-up)
         tmem_ld8(tbase + kResTmemAp + 8u * k, zk);
 #pragma unroll
         for (int z = 0; z < 8; ++z) P.v[z] = tadd(zk[z], tmul(fbeta, P.v[z]));  // pnew_of's operations
-        ps_stcol(ps, hl >> 1, h.c, P);
+        ps_st4(ps, own, P);
         if ((mir >> k) & 1u) stcol(pm_new, unsigned(h.s) * 512u + unsigned(h.c), P);
       }
     }
@@ -2335,7 +2335,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         const HalfLeaf h = half_pos(2 * fr.L0 + hl, lane);
         const int ol = (hl >> 1) * 512 + h.c;
         Col<float> P, ap;
-        ps_ldcol(ps, hl >> 1, h.c, P);
+        ps_ld4(ps, ps_col4(hl >> 1, h.xb + h.lx, h.cy), P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
         res_ap(fr, a, pm_old, tab, fbeta, h.s, h.xb, h.lx, h.cy, lane, fs, P, f, ap);
 #pragma unroll
@@ -2372,7 +2372,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
           tmem_ld8(txb, X.v);
         else
           xs_ld(xs, k, warp, lane, X.v);
-        ps_ldcol(ps, hl >> 1, h.c, P);
+        ps_ld4(ps, ps_col4(hl >> 1, h.xb + h.lx, h.cy), P);
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + ol);
 #pragma unroll
         for (int z = 0; z < 8; ++z) X.v[z] = tadd(tmul(fa, P.v[z]), X.v[z]);
