@@ -1905,12 +1905,14 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1_s(const __grid_const
 //      columns other CTAs read into a global mirror), then A p (kept) and
 //      the p.Ap partials;
 //   grid barrier: every CTA sums the G partials in CTA order -> alpha;
-//   U: x += alpha p, r -= alpha A p (the columns other CTAs read also into a
-//      global mirror), the r.r and r.z partials;
+//   U: x += alpha p, r -= alpha A p, z = M r (of the columns other CTAs read
+//      also into a global mirror), the r.r and r.z partials;
 //   grid barrier -> r.r, r.z, beta and the loop test.
+// (One more grid barrier before the first iteration publishes the first z.)
 // Stencil neighbours in the CTA's own leaves come from shared memory; those
-// in other CTAs' leaves are formed from the mirrors of r and the previous p,
-// read through L2 (the owner's operations, so the owner's bits; p alternates
+// in other CTAs' leaves are formed as z + beta p from the mirrors of z and
+// the previous p, read through L2 (the owner's operations, so the owner's
+// bits; p alternates
 // between two mirror buffers by iteration parity), by all 32 lanes of the
 // warp together and handed out by warp shuffles.  A p is summed in the
 // reference's column order.  The dot products are summed per thread, per
@@ -2051,21 +2053,21 @@ __device__ __forceinline__ bool res_local(const ResFrame& fr, int slot) {
 }
 
 // p (current iteration) of cell (x, y, z) of leaf `slot`: from shared memory
-// for the CTA's leaves, else formed from the mirrors of r and the previous p.
+// for the CTA's leaves, else formed from the mirrors of z and the previous p.
 __device__ __forceinline__ float res_pcell(const ResFrame& fr, const PcgArgs& a,
                                            const float* pm_old, const DiagInv<float>* tab,
                                            float beta, int slot, int x, int y, int z) {
   if (res_local(fr, slot)) return fr.ps[(ps_col4(slot - fr.L0, x, y) + (z >> 2) * 64) * 4 + (z & 3)];
   const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(x * 64 + y * 8 + z);
-  return pnew_of<float>(tab, a.flags[o], __ldcg(static_cast<const float*>(a.r) + o),
-                        __ldcg(pm_old + o), beta);
+  // the mirror holds z = M r (the owner's product): pnew_of's operations
+  return tadd(__ldcg(static_cast<const float*>(a.r) + o), tmul(beta, __ldcg(pm_old + o)));
 }
 
 // The half leaf's faces in other CTAs' leaves (its outward x face and both
 // y faces: 16 columns of 8 cells), formed by all 32 lanes in step: lane L
 // forms cells 4 (L & 1) .. + 3 of face column t = L >> 1 (t < 8: the x face
 // at y = t; 8 .. 11: the -y face at x = xb + t - 8; 12 .. 15: the +y face)
-// from the mirrors of r and the previous p, with the owner's operations.
+// from the mirrors of z and the previous p, with the owner's operations.
 // Faces in the CTA's own leaves are left to shared memory (v stays 0).
 __device__ __forceinline__ void res_faces(const ResFrame& fr, const PcgArgs& a, const float* pm_old,
                                           const DiagInv<float>* tab, float beta, int xb,
@@ -2087,13 +2089,13 @@ __device__ __forceinline__ void res_faces(const ResFrame& fr, const PcgArgs& a, 
   for (int j = 0; j < 4; ++j) v[j] = 0.f;
   if (!res_local(fr, slot)) {
     const unsigned o = slot_or_null(slot, fr.n_pleaf) * 512u + unsigned(off);
-    const float4 r = __ldcg(reinterpret_cast<const float4*>(static_cast<const float*>(a.r) + o));
+    // the mirror holds z = M r (the owner's product): pnew_of's operations
+    const float4 zm = __ldcg(reinterpret_cast<const float4*>(static_cast<const float*>(a.r) + o));
     const float4 po = __ldcg(reinterpret_cast<const float4*>(pm_old + o));
-    const unsigned f = __ldg(reinterpret_cast<const unsigned*>(a.flags + o));
-    v[0] = pnew_of<float>(tab, uint8_t(f), r.x, po.x, beta);
-    v[1] = pnew_of<float>(tab, uint8_t(f >> 8), r.y, po.y, beta);
-    v[2] = pnew_of<float>(tab, uint8_t(f >> 16), r.z, po.z, beta);
-    v[3] = pnew_of<float>(tab, uint8_t(f >> 24), r.w, po.w, beta);
+    v[0] = tadd(zm.x, tmul(beta, po.x));
+    v[1] = tadd(zm.y, tmul(beta, po.y));
+    v[2] = tadd(zm.z, tmul(beta, po.z));
+    v[3] = tadd(zm.w, tmul(beta, po.w));
   }
 }
 // column c of the faces formed by res_faces (lanes 2 c and 2 c + 1)
@@ -2264,12 +2266,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
       Col<float> r0;
       ldcol(static_cast<const float*>(a.r), og, r0);
       tmem_st8(tbase + 8u * k, r0.v);
+      Col<float> z0;
       {
         const uint2 f = *reinterpret_cast<const uint2*>(fsm + (hl >> 1) * 512 + h.c);
-        float z0[8];
 #pragma unroll
-        for (int z = 0; z < 8; ++z) z0[z] = tmul(tab[fbyte(f, z) & 15].inv, r0.v[z]);
-        tmem_st8(tbase + kResTmemAp + 8u * k, z0);
+        for (int z = 0; z < 8; ++z) z0.v[z] = tmul(tab[fbyte(f, z) & 15].inv, r0.v[z]);
+        tmem_st8(tbase + kResTmemAp + 8u * k, z0.v);
       }
       ldcol(static_cast<const float*>(a.x), og, r0);
       if (k == 0)
@@ -2283,7 +2285,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
                                 : (h.lx == 3 && !res_local(fr, fs[1]));
       const bool yo = (h.cy == 0 && !res_local(fr, fs[2])) || (h.cy == 7 && !res_local(fr, fs[3]));
       const bool zo = !res_local(fr, fs[4]) || !res_local(fr, fs[5]);
-      if (xo || yo || zo) mir |= 1u << k;
+      if (xo || yo || zo) {
+        mir |= 1u << k;
+        stcol(static_cast<float*>(a.r), og, z0);  // the mirror of z for the first iteration
+      }
     }
   }
   tmem_wait_st();
@@ -2302,8 +2307,13 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
   unsigned round = 0;
   bool ok = true;
   float* x = static_cast<float*>(a.x);
-  float* rmir = static_cast<float*>(a.r);
-  while (!s_done) {
+  float* rmir = static_cast<float*>(a.r);  // during the loop: the mirror of z = M r
+  {
+    // every CTA's z mirror is written before any CTA's first stencil reads it
+    float v[1] = {0.f};
+    ok = res_sync<1>(a, v, 0, ++round, &s_ok, [](const double (&)[1]) {});
+  }
+  while (ok && !s_done) {
     float* pm_new = static_cast<float*>((it & 1) ? a.p1 : a.p0);
     const float* pm_old = static_cast<const float*>((it & 1) ? a.p0 : a.p1);
     const float fbeta = s_fbeta;
@@ -2393,7 +2403,12 @@ __global__ void __launch_bounds__(kResThreads, 1) k_pcg_resident(const __grid_co
         }
         tmem_st8(tbase + 8u * k, R.v);
         tmem_st8(tbase + kResTmemAp + 8u * k, ap);
-        if ((mir >> k) & 1u) stcol(rmir, og, R);
+        if ((mir >> k) & 1u) {
+          Col<float> Z;
+#pragma unroll
+          for (int z = 0; z < 8; ++z) Z.v[z] = ap[z];
+          stcol(rmir, og, Z);
+        }
       }
     }
     tmem_wait_st();
