@@ -1912,9 +1912,8 @@ __global__ void __launch_bounds__(kHotThreads, 4) k_pcg_cg1_s(const __grid_const
 // Stencil neighbours in the CTA's own leaves come from shared memory; those
 // in other CTAs' leaves are formed as z + beta p from the mirrors of z and
 // the previous p, read through L2 (the owner's operations, so the owner's
-// bits; p alternates
-// between two mirror buffers by iteration parity), by all 32 lanes of the
-// warp together and handed out by warp shuffles.  A p is summed in the
+// bits; p alternates between two mirror buffers by iteration parity), by all
+// 32 lanes of the warp together and handed out by warp shuffles.  A p is summed in the
 // reference's column order.  The dot products are summed per thread, per
 // CTA and over CTAs in fixed orders: the solve is deterministic (its
 // per-thread order differs from the pair's, so the bits do too).  Thread 0
