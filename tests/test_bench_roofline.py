@@ -49,6 +49,23 @@ def test_mixed_pair_and_other_kernels():
     assert r["kernel"] == "p2g_fused" and r["frac"] is None
 
 
+def test_resident_loop_is_one_iteration():
+    """The resident loop is one launch per solve; its iteration is counted in
+    the pair's 34 B per unknown, and its traffic is the measured DRAM bytes
+    per iteration, with a note that frac above 1 is expected."""
+    kt = {"pcg_resident": (25.0, 1), "p2g_fused": (1.5, 1)}
+    r = bench.roofline(_res(kt, [12.0, 13.0]))
+    assert r["kernel"] == "pcg_iteration (pcg_resident, one cooperative launch per solve)"
+    assert r["alg_bytes_per_unknown"] == 34
+    tot = 34 * (4_000_000 * 700 + 4_100_000 * 800)
+    assert r["achieved"] == pytest.approx(tot / 25.0e-3 / 1e9)
+    assert r["us_per_iteration"] == pytest.approx(25.0e3 / 1500)
+    assert r["traffic"] == pytest.approx(bench.NCU_TRAFFIC_PER_UNKNOWN["pcg_resident"] * 4_050_000)
+    assert r["traffic"] < 1e-3 * r["alg_bytes_per_launch"]  # on chip: almost no DRAM traffic
+    assert "on chip" in r["note"]
+    assert set(r["per_kernel_profiled"]) == {"pcg_resident"}
+
+
 def test_whole_job_rate_counts_every_replica():
     assert bench.whole_job_rate(4, 20, 1000.0) == pytest.approx(80.0)
 
