@@ -76,14 +76,14 @@ UNFUSED_BYTES = {"pcg_spmv": 50, "pcg_spmv_mixed": 50, "pcg_cg1": 50, "pcg_resid
 # the timed loop, where the vectors stay in L2 and DRAM mostly sees write-backs.  Scaled by
 # each step's unknowns.  The MIXED pair: a capture at 1024^3 (111,452,816 unknowns, caches
 # flushed; the vectors do not fit in L2 there), the size its solver is benchmarked at.
-# The resident loop: one launch is a whole solve, so its DRAM bytes (48.42 MB read + 23.55 MB
+# The resident loop: one launch is a whole solve, so its DRAM bytes (48.22 MB read + 23.18 MB
 # written) are divided by the solve's 779 iterations: a capture of the timed step of the
 # 256^3 dam break (about 4.03 M unknowns) with the default bench settings.
 NCU_TRAFFIC_PER_UNKNOWN = {"pcg_spmv": (1.4706e6 + 17.5451e6) / 4021250,
                            "pcg_update": (5.4866e6 + 19.9465e6) / 4021250,
                            "pcg_spmv_mixed": 1.5765e9 / 111452816,
                            "pcg_update_mixed": 2.3834e9 / 111452816,
-                           "pcg_resident": (48.420352e6 + 23.554048e6) / 779 / 4.03e6}
+                           "pcg_resident": (48.224768e6 + 23.182592e6) / 779 / 4.03e6}
 NCU_TRAFFIC_SOURCE = {"pcg_spmv": "the 256^3 system, caches not flushed",
                       "pcg_update": "the 256^3 system, caches not flushed",
                       "pcg_spmv_mixed": "the 1024^3 system, caches flushed",
